@@ -1,0 +1,368 @@
+#!/usr/bin/env python
+"""Throughput of the GB300 wind-tunnel step in cell-steps/s.
+
+Workload: the reference's default tunnel, 1920x1080, n=50 red/black sweeps,
+viscosity 0.001 (n Jacobi diffusion sweeps), smoke on, drain on, g=-5,
+dt=0.05, seeded uniform[-0.01, 0.01] velocity perturbation (synthetic: the
+reference has no dataset). A step is one Fluid::update.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+value  : W*H*K / (sum of the K per-step CUDA-event times), fields resident in
+         HBM, L2 flushed between steps (a 256 MiB write outside the timed
+         events; the step's own working set fits in the 129 MB L2).
+e2e    : the same metric through the C ABI as the reference's frame loop uses
+         it: a synchronous os_update() (whose new d_t goes host->device) and a
+         device->host read of the smoke field into pinned memory, every step.
+N > 1  : independent replicas, one grid per GPU (the path does not shard);
+         value = all ranks' cell-steps / the slowest rank's time.
+--impl reference: the reference's per-cell update as a CPU loop on all host
+         cores (the oracle port; the reference has no CPU build of its own),
+         plus, where a GPU is present, the reference's own CUDA kernels driven
+         as its Fluid::update drives them.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "cell-steps/s (incl. n sweeps) 1920x1080 & batched; serve p50/p99 vs plain, same GPU"
+UNIT = "cell-steps/s"
+FALLBACK_HBM_GBS = 6800.0
+L2_FLUSH_BYTES = 256 << 20
+
+
+def peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    return {"hbm_gbs": FALLBACK_HBM_GBS, "source": "fallback"}
+
+
+def bytes_per_cell_step(n: int, viscous: bool) -> int:
+    """Compulsory FP32 traffic of an unfused phase-per-pass schedule (1-byte
+    flags): forces 8, diffusion 8/sweep, projection 17/sweep, advection 17+17."""
+    return (25 if viscous else 17) * n + 42
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    NAMES = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(self.gpu)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        self.samples = []
+        if self.proc is None:
+            return
+        time.sleep(0.3)
+        self.proc.terminate()
+        out, _ = self.proc.communicate(timeout=10)
+        for line in out.strip().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                self.samples.append(parts)
+
+    def summary(self) -> dict:
+        if not getattr(self, "samples", None):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        reasons = set()
+        for s in self.samples:
+            for name, val in zip(self.NAMES, s[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.samples)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        dist.init_process_group(backend=backend)
+    return world, rank, local
+
+
+def dist_barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def dist_max(world, x: float) -> float:
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if torch.cuda.is_available() and dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_baseline(cfg, budget_s: float = 12.0, max_steps: int = 60) -> dict:
+    """The oracle port on the host cores (rank 0, N=1 only)."""
+    import oracle
+    from opensayal_gb300 import scenarios
+    o = oracle.OracleFluid(cfg)
+    u, v = scenarios.perturbation(2, o.is_solid)
+    o.u[:], o.v[:] = u, v
+    o.update(None, cfg.d_t)  # first touch of the working set
+    steps, t0 = 0, time.perf_counter()
+    while steps < max_steps:
+        o.update(None, cfg.d_t)
+        steps += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    el = time.perf_counter() - t0
+    return {"value": cfg.width * cfg.height * steps / el, "unit": UNIT,
+            "cores": oracle.oracle_threads(), "kind": "port",
+            "sample": f"{steps} full {cfg.width}x{cfg.height} steps of the C/OpenMP restatement "
+                      f"({el:.1f} s)"}
+
+
+def workload_config(name: str):
+    from opensayal_gb300 import scenarios
+    return {"default": scenarios.default_tunnel_config, "small": scenarios.small_config,
+            "large": scenarios.large_config}[name]()
+
+
+def config_record(cfg, name: str, extra: dict) -> dict:
+    rec = {"workload": f"{name}: {cfg.width}x{cfg.height} tunnel, n={cfg.projection_n}, "
+                       f"o={cfg.projection_o:g}, viscosity={cfg.viscosity:g}, g={cfg.g:g}, "
+                       f"dt={cfg.d_t:g}, drain={cfg.enable_drain}, smoke={cfg.enable_smoke}",
+           "width": cfg.width, "height": cfg.height, "projection_n": cfg.projection_n,
+           "storage": ["f32", "f16", "bf16", "f64"][cfg.storage],
+           "l2": "flushed between steps (256 MiB write outside the timed events)"}
+    rec.update(extra)
+    return rec
+
+
+def run_gb300(args, world, rank, local) -> dict | None:
+    import torch
+    from opensayal_gb300 import Fluid, native, scenarios
+    from opensayal_gb300.build import build_library
+    build_library()
+    torch.cuda.set_device(local)
+    cfg = workload_config(args.workload)
+    cfg.device = local
+    if args.block is not None:
+        cfg.projection_block = args.block
+    cells = cfg.width * cfg.height
+    f = Fluid(cfg)
+    u, v = scenarios.perturbation(2, f.download("is_solid"))
+    f.upload("vel_x", u)
+    f.upload("vel_y", v)
+    stream = torch.cuda.Stream()
+    sptr = stream.cuda_stream
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    dt = cfg.d_t
+    with torch.cuda.stream(stream):
+        f.update_async(None, dt, max(args.warmup, 3), sptr)
+    stream.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    launches0 = f.kernel_launches
+    dist_barrier(world)
+    torch.cuda.synchronize()
+    with Clocks(local) as clk:
+        wall0 = time.perf_counter()
+        with torch.cuda.stream(stream):
+            for k in range(args.steps):
+                flush.add_(1.0)
+                starts[k].record(stream)
+                f.update_async(None, dt, 1, sptr)
+                ends[k].record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - wall0
+    dist_barrier(world)
+    launches = f.kernel_launches - launches0
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_s = dist_max(world, sum(step_ms) / 1e3)
+    value = world * cells * args.steps / total_s
+
+    # e2e: synchronous update + smoke read-back into pinned memory, per step
+    pinned = torch.empty(cells, dtype=torch.float32, pin_memory=True).numpy()
+    dts = [dt, float(np.nextafter(np.float32(dt), np.float32(1.0)))]
+    e2e_steps = args.steps
+    f.update(None, dts[1])
+    dist_barrier(world)
+    t0 = time.perf_counter()
+    for k in range(e2e_steps):
+        f.update(None, dts[k & 1])
+        f.download("smoke", out=pinned)
+    e2e_s = dist_max(world, time.perf_counter() - t0)
+    e2e = {"value": world * cells * e2e_steps / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": 32, "d2h_bytes_per_step": 4 * cells}
+
+    # roofline of the dominant phase (projection), timed alone on the same stream
+    pk = peaks()
+    proj_ms, proj_kernels = f.profile_phase(native.PHASE_PROJECTION, None, dt, 3, sptr)
+    proj_s = proj_ms / 3 / 1e3
+    proj_bytes = 17 * cfg.projection_n * cells
+    diff_ms, diff_kernels = f.profile_phase(native.PHASE_DIFFUSION, None, dt, 3, sptr)
+    achieved = proj_bytes / proj_s / 1e9
+    traffic = None
+    tfile = ROOT / "profiles" / "roofline_traffic.json"
+    if tfile.exists():
+        t = json.loads(tfile.read_text()).get(f"{args.workload}:block{cfg.projection_block}")
+        traffic = t
+    step_bytes = bytes_per_cell_step(cfg.projection_n, cfg.viscosity != 0.0)
+    ms_per_step = total_s * 1e3 / args.steps
+    result = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": ["f32", "f16", "bf16", "f64"][cfg.storage], "data": "synthetic",
+        "config": config_record(cfg, args.workload, {
+            "parallelism": "replicas" if world > 1 else "single", "global_batch": world,
+            "kernels_per_step": launches // max(1, args.steps),
+            "projection_block": cfg.projection_block}),
+        "e2e": e2e,
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"],
+                     "unit": "GB/s", "frac": achieved / pk["hbm_gbs"], "traffic": traffic,
+                     "kernel": "projection phase (17 B/cell per red/black sweep x n sweeps)",
+                     "launches": proj_kernels // 3, "peak_source": pk["source"]},
+        "step_roofline": {"bytes_per_cell_step": step_bytes,
+                          "achieved": step_bytes * value / world / 1e9, "unit": "GB/s",
+                          "frac": step_bytes * value / world / 1e9 / pk["hbm_gbs"]},
+        "phase_ms": {"projection": proj_ms / 3, "diffusion": diff_ms / 3},
+        "wall_s": wall,
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        result["cpu_baseline"] = cpu_baseline(cfg)
+    f.close()
+    return result if rank == 0 else None
+
+
+def run_reference(args, world, rank, local) -> dict | None:
+    if rank != 0:
+        return None
+    import oracle
+    from opensayal_gb300 import scenarios
+    cfg = workload_config(args.workload)
+    cells = cfg.width * cfg.height
+    o = oracle.OracleFluid(cfg)
+    u, v = scenarios.perturbation(2, o.is_solid)
+    o.u[:], o.v[:] = u, v
+    for _ in range(min(args.warmup, 1)):
+        o.update(None, cfg.d_t)
+    budget = 150.0
+    t0 = time.perf_counter()
+    done = 0
+    while done < args.steps:
+        o.update(None, cfg.d_t)
+        done += 1
+        if time.perf_counter() - t0 > budget:
+            break
+    el = time.perf_counter() - t0
+    value = cells * done / el
+    sample = (f"{done} of {args.steps} requested full {cfg.width}x{cfg.height} steps "
+              f"({el:.1f} s; capped at {budget:.0f} s)")
+    result = {
+        "metric": METRIC, "value": value, "unit": UNIT, "impl": "reference",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": el * 1e3 / done, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": config_record(cfg, args.workload, {"parallelism": "host cores"}),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": oracle.oracle_threads(),
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    result["reference_cuda"] = reference_cuda(cfg, args)
+    return result
+
+
+def reference_cuda(cfg, args) -> dict:
+    """The reference's own kernels (unmodified src/fluid.cu device code), driven
+    with its launch shapes and its per-step device synchronisation."""
+    import oracle
+    try:
+        import torch
+        if not torch.cuda.is_available() or not oracle.reference_available():
+            return {"unavailable": "no GPU or no reference cubin"}
+        from opensayal_gb300 import scenarios
+        r = oracle.RefFluid(cfg)
+        u, v = scenarios.perturbation(2, r.is_solid)
+        r.upload("vel_x", u)
+        r.upload("vel_y", v)
+        for _ in range(max(args.warmup, 3)):
+            r.update(None, cfg.d_t)
+        steps = min(args.steps, 200)
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            r.update(None, cfg.d_t)
+        el = time.perf_counter() - t0
+        r.close()
+        return {"value": cfg.width * cfg.height * steps / el, "unit": UNIT, "steps": steps,
+                "ms_per_step": el * 1e3 / steps,
+                "timing": "host wall clock around Fluid::update, which synchronises each step"}
+    except Exception as exc:  # the arm must still print its line
+        return {"unavailable": f"{type(exc).__name__}: {exc}"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="default", choices=["default", "small", "large"])
+    ap.add_argument("--block", type=int, default=None,
+                    help="red/black sweeps per blocked pass (0 autotune, -1 plain)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        res = run_reference(args, world, rank, local)
+    else:
+        res = run_gb300(args, world, rank, local)
+    if res is not None:
+        print(json.dumps(res), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,234 @@
+/*
+ * opensayal_gb300.h — C ABI of the GB300 wind-tunnel simulation step.
+ *
+ * This library is a drop-in for OpenSayal's `Fluid` class (inc/fluid.cuh:15-116,
+ * src/fluid.cu): the same constructor keys, the same per-frame update, the same
+ * field layout. Everything is plain C: pointers, sizes and status codes, no C++
+ * or torch types, so any FFI (ctypes, cgo, JNI, N-API) can bind it. A C++
+ * `class Fluid` with the reference's public members is layered on top in
+ * include/opensayal_gb300/fluid.hpp.
+ *
+ * Field layout (identical to the reference, src/fluid.cu:163-165): every field
+ * is a width*height array indexed by indx(i, j) = (height - 1 - j) * width + i,
+ * i.e. row-major with j = 0 (the bottom row) stored last. u(i, j) lives on the
+ * left face of cell (i, j), v(i, j) on its bottom face, smoke and pressure at
+ * the centre.
+ *
+ * Errors: every entry point returns an os_status. On failure a description is
+ * available from os_last_error() (thread-local). The library never calls exit().
+ *
+ * Threading: one handle must not be used from two host threads at once (the
+ * reference's Fluid is not re-entrant either). Distinct handles are independent.
+ */
+#ifndef OPENSAYAL_GB300_H
+#define OPENSAYAL_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define OS_ABI_VERSION 1
+
+typedef enum os_status {
+  OS_OK = 0,
+  OS_ERR_INVALID = 1,     /* bad argument or configuration */
+  OS_ERR_CUDA = 2,        /* a CUDA runtime call failed */
+  OS_ERR_NOMEM = 3,       /* device or host allocation failed */
+  OS_ERR_UNSUPPORTED = 4, /* valid request this build does not implement */
+  OS_ERR_STATE = 5,       /* call not valid in the handle's current state */
+  OS_ERR_TIMEOUT = 6      /* a bounded device wait gave up */
+} os_status;
+
+/* Field identifiers for os_upload / os_download. */
+typedef enum os_field {
+  OS_FIELD_VEL_X = 0,    /* Fluid::d_vel_x   (float) */
+  OS_FIELD_VEL_Y = 1,    /* Fluid::d_vel_y   (float) */
+  OS_FIELD_SMOKE = 2,    /* Fluid::d_smoke   (float) */
+  OS_FIELD_PRESSURE = 3, /* Fluid::d_pressure (float) */
+  OS_FIELD_IS_SOLID = 4, /* Fluid::d_is_solid (int32, read-only) */
+  OS_FIELD_TOTAL_S = 5   /* Fluid::d_total_s  (int32, read-only) */
+} os_field;
+
+/* Storage precision of u, v and smoke. FP32 is the reference's precision. */
+typedef enum os_storage {
+  OS_STORAGE_F32 = 0,  /* the reference's precision */
+  OS_STORAGE_F16 = 1,  /* FP16 u, v, smoke; FP32 arithmetic */
+  OS_STORAGE_BF16 = 2, /* BF16 u, v, smoke; FP32 arithmetic */
+  OS_STORAGE_F64 = 3   /* FP64 storage and arithmetic: the error yardstick */
+} os_storage;
+
+/*
+ * Flat mirror of the reference's `Config` (inc/config_parser.hpp:9-115): the
+ * thread.cuda, sim and fluid keys that Fluid reads (src/fluid.cu:41-71,111-126).
+ * Visual and OpenMP keys do not reach the simulation and are not carried.
+ * Booleans are int32 (0 / non-zero). Fill it with os_config_defaults() and then
+ * override keys, exactly like an OpenSayal.conf.json overrides the parser's
+ * defaults.
+ */
+typedef struct os_config {
+  /* thread.cuda.block_size_{x,y} (config_parser.cpp:30-33). Kept so that the
+   * C++ wrapper can expose kernel_grid_dim/kernel_block_dim; the GB300 kernels
+   * choose their own launch shapes. */
+  int32_t block_size_x;
+  int32_t block_size_y;
+  /* sim.* */
+  int32_t height;
+  int32_t width;
+  int32_t cell_pixel_size;
+  float cell_size; /* truncated to int, as Fluid::cell_size is (inc/fluid.cuh:46) */
+  int32_t enable_drain;
+  int32_t enable_pressure;
+  int32_t enable_smoke;
+  int32_t enable_interactive;
+  int32_t projection_n;  /* sim.projection.n */
+  float projection_o;    /* sim.projection.o */
+  int32_t pipe_height;   /* sim.wind_tunnel.pipe_height */
+  int32_t pipe_length;   /* sim.wind_tunnel.pipe_length (parser hard-codes 0) */
+  int32_t smoke_length;  /* sim.wind_tunnel.smoke_length */
+  int32_t smoke_height;  /* sim.wind_tunnel.smoke_height */
+  int32_t smoke_count;   /* sim.wind_tunnel.smoke_count */
+  float tunnel_speed;    /* sim.wind_tunnel.speed */
+  float tunnel_smoke;    /* sim.wind_tunnel.smoke */
+  float g;               /* sim.physics.g */
+  float d_t;             /* sim.time.d_t */
+  int32_t enable_real_time;
+  float real_time_multiplier;
+  int32_t smoke_enable_decay; /* sim.smoke.enable_decay */
+  float smoke_decay_rate;     /* sim.smoke.decay_rate */
+  int32_t obstacle_enable;
+  int32_t obstacle_center_x;
+  int32_t obstacle_center_y;
+  float obstacle_radius;
+  /* fluid.* */
+  float density;
+  float drag_coeff;
+  float viscosity;
+  /* Extensions with no reference key. Zero means "reference behaviour". */
+  int32_t storage;          /* os_storage of u, v, smoke; 0 = FP32 */
+  int32_t device;           /* CUDA device ordinal */
+  int32_t projection_block; /* red/black sweeps fused per pass; 0 = autotune,
+                               -1 = one launch per half-sweep (plain form) */
+  int32_t fast_idw;         /* 1: smoke inverse-distance weights in FP32; 0
+                               (default): in FP64 as the reference computes
+                               them (src/fluid.cu:690-693) */
+  int32_t reserved[4];
+} os_config;
+
+/* The reference's `Source` (inc/fluid.cuh:8-13), the interactive forcing. */
+typedef struct os_source {
+  int32_t active;
+  float smoke;
+  float velocity;
+  int32_t position_x;
+  int32_t position_y;
+} os_source;
+
+/* Device pointers of a handle's public fields, laid out by indx(i, j). */
+typedef struct os_fields_view {
+  int32_t width;
+  int32_t height;
+  int32_t storage;    /* os_storage of vel_x, vel_y, smoke */
+  int32_t reserved;
+  void* vel_x;        /* Fluid::d_vel_x */
+  void* vel_y;        /* Fluid::d_vel_y */
+  void* smoke;        /* Fluid::d_smoke */
+  float* pressure;    /* Fluid::d_pressure */
+  int32_t* is_solid;  /* Fluid::d_is_solid */
+  int32_t* total_s;   /* Fluid::d_total_s */
+} os_fields_view;
+
+typedef struct os_handle os_handle;
+
+/* ABI version of the loaded library (OS_ABI_VERSION). */
+int32_t os_abi_version(void);
+
+/* Human-readable description of the last failure on this host thread. */
+const char* os_last_error(void);
+
+/*
+ * ConfigParser defaults for a width x height tunnel (src/config_parser.cpp:
+ * 15-184): pipe_height = smoke_height = height/4, obstacle at the centre with
+ * radius min(w, h)/30, viscosity 0.001, n = 50, o = 1.9, drain and smoke on.
+ * Replaces: ConfigParser::parse() with an empty JSON object.
+ */
+int os_config_defaults(int32_t width, int32_t height, os_config* out);
+
+/*
+ * Allocates the fields, rasterises the solid mask and neighbour counts, zeroes
+ * u, v, smoke and pressure. Replaces: Fluid::Fluid(Config) (src/fluid.cu:41-71,
+ * 86-161). Unlike the reference it validates the configuration and reports
+ * failures instead of proceeding with undefined state.
+ */
+int os_create(const os_config* cfg, os_handle** out);
+
+/* Frees every device array. Replaces: Fluid::~Fluid() (src/fluid.cu:73-84). */
+int os_destroy(os_handle* h);
+
+/*
+ * One simulation step, synchronous like the reference (it ends with a device
+ * synchronisation). Replaces: Fluid::update(Source, float) (src/fluid.cu:
+ * 770-795). `src` may be NULL for an inactive source.
+ */
+int os_update(os_handle* h, const os_source* src, float dt);
+
+/*
+ * `steps` simulation steps enqueued on `stream` (a cudaStream_t, NULL for the
+ * handle's own stream) without synchronising; replays one captured CUDA graph
+ * per step. No reference counterpart (the reference synchronises every step).
+ */
+int os_update_async(os_handle* h, const os_source* src, float dt,
+                    int32_t steps, void* stream);
+
+/* Waits for all work enqueued on the handle's stream. */
+int os_synchronize(os_handle* h);
+
+/* Device pointers of the public fields. Replaces: reading Fluid::d_* members. */
+int os_fields(os_handle* h, os_fields_view* out);
+
+/* Host <-> device copies of one field; `count` must equal width*height.
+ * Float fields are converted from / to the storage precision. */
+int os_upload(os_handle* h, int32_t field, const void* host, size_t count);
+int os_download(os_handle* h, int32_t field, void* host, size_t count);
+
+/* Pressure extrema of the last step with enable_pressure set.
+ * Replaces: Fluid::min_pressure / Fluid::max_pressure (src/fluid.cu:778-787). */
+int os_pressure_range(os_handle* h, float* min_out, float* max_out);
+
+/*
+ * Runs one phase of the step on the current fields (diagnostics and phase-level
+ * parity tests). Replaces the private phase methods of Fluid
+ * (src/fluid.cu:185-190,216-219,282-295,351-354,591-596,637-642,744-747,764-767).
+ */
+typedef enum os_phase {
+  OS_PHASE_FORCES = 0,         /* apply_external_forces */
+  OS_PHASE_ZERO_PRESSURE = 1,  /* zero_pressure */
+  OS_PHASE_DIFFUSION = 2,      /* apply_diffusion: n sweeps */
+  OS_PHASE_PROJECTION = 3,     /* apply_projection: n red/black sweeps */
+  OS_PHASE_PRESSURE_RANGE = 4, /* min/max reduction of pressure */
+  OS_PHASE_EXTRAPOLATION = 5,  /* apply_extrapolation */
+  OS_PHASE_VEL_ADVECTION = 6,  /* apply_velocity_advection (+ copy back) */
+  OS_PHASE_SMOKE_ADVECTION = 7,/* apply_smoke_advection (+ copy back) */
+  OS_PHASE_DECAY = 8           /* decay_smoke */
+} os_phase;
+int os_run_phase(os_handle* h, int32_t phase, const os_source* src, float dt);
+
+/* Number of kernels this library launched on the handle since creation. */
+int os_kernel_launches(os_handle* h, int64_t* out);
+
+/*
+ * Diagnostics: enqueues `reps` repetitions of one phase on `stream` (NULL for
+ * the handle's own stream) between two CUDA events recorded on that stream,
+ * waits, and returns the elapsed milliseconds and the number of kernels the
+ * repetitions launched. No reference counterpart.
+ */
+int os_profile_phase(os_handle* h, int32_t phase, const os_source* src, float dt,
+                     int32_t reps, void* stream, float* ms_out, int32_t* kernels_out);
+
+#ifdef __cplusplus
+}  /* extern "C" */
+#endif
+
+#endif /* OPENSAYAL_GB300_H */

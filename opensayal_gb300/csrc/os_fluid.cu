@@ -1,0 +1,693 @@
+// os_fluid.cu — host side of the GB300 wind tunnel: handle lifecycle, the
+// captured per-step CUDA graph, and the C ABI declared in
+// include/opensayal_gb300.h.
+//
+// One handle = one grid = the reference's Fluid object (inc/fluid.cuh:15-116).
+// Its fields live in device memory in the reference's layout for the whole
+// life of the handle; a step is one replay of a CUDA graph captured at the
+// first update (the reference launches ~157 kernels per step on the legacy
+// stream and synchronises, src/fluid.cu:770-795). Per-step inputs (dt and the
+// Source) sit in a device-side StepParams block that is refreshed only when
+// they change, so one graph serves every step.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "../../include/opensayal_gb300.h"
+#include "os_kernels.cuh"
+
+using namespace osg;
+
+namespace {
+
+thread_local char g_err[512] = "";
+
+int set_err(int code, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof g_err, fmt, ap);
+  va_end(ap);
+  return code;
+}
+
+#define CUDA_OR_RETURN(expr)                                                    \
+  do {                                                                          \
+    cudaError_t e_ = (expr);                                                    \
+    if (e_ != cudaSuccess)                                                      \
+      return set_err(OS_ERR_CUDA, "%s failed: %s", #expr, cudaGetErrorString(e_)); \
+  } while (0)
+
+size_t storage_bytes(int storage) {
+  switch (storage) {
+    case OS_STORAGE_F32: return 4;
+    case OS_STORAGE_F16: return 2;
+    case OS_STORAGE_BF16: return 2;
+    case OS_STORAGE_F64: return 8;
+    default: return 0;
+  }
+}
+
+}  // namespace
+
+struct os_handle {
+  os_config cfg;
+  Consts c;
+  int W = 0, H = 0;
+  size_t N = 0;
+  int storage = OS_STORAGE_F32;
+  size_t esize = 4;
+  int smoke_period = 1;
+  int block_k = 0;  // red/black sweeps per blocked pass; -1: plain form
+  cudaStream_t stream = nullptr;
+  // fields (reference layout); u, v, s in storage precision
+  void *u = nullptr, *v = nullptr, *s = nullptr;
+  void *ub = nullptr, *vb = nullptr, *sb = nullptr;
+  float* p = nullptr;
+  int32_t *is_solid = nullptr, *total_s = nullptr;
+  uint8_t* flags = nullptr;
+  StepParams* d_params = nullptr;
+  StepParams* h_params = nullptr;        // pinned staging slot
+  cudaEvent_t params_event = nullptr;    // completion of the last copy out of it
+  int64_t params_bytes = 0;              // host->device parameter bytes so far
+  StepParams last_params;
+  bool params_valid = false;
+  int* d_pkeys = nullptr;   // pressure extrema as ordered integer keys
+  int* h_pkeys = nullptr;   // pinned copy
+  float* conv = nullptr;    // FP32 staging for non-FP32 storage transfers
+  cudaGraphExec_t graph = nullptr;
+  int kernels_per_step = 0;
+  int64_t launches = 0;
+  float min_pressure = 0.0f, max_pressure = 0.0f;
+};
+
+// The temporally blocked projection/diffusion engine works on the handle.
+#include "os_blocked.cuh"
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// Step enqueue (captured into the graph).
+// ---------------------------------------------------------------------------
+
+struct Enq {
+  cudaStream_t st;
+  int count = 0;
+};
+
+template <class S, class A>
+int enqueue_phase(os_handle* h, int phase, Enq& q) {
+  const Consts& c = h->c;
+  S* u = static_cast<S*>(h->u);
+  S* v = static_cast<S*>(h->v);
+  S* s = static_cast<S*>(h->s);
+  S* ub = static_cast<S*>(h->ub);
+  S* vb = static_cast<S*>(h->vb);
+  S* sb = static_cast<S*>(h->sb);
+  const int W = h->W, H = h->H;
+  const int64_t N = (int64_t)h->N;
+  const int T = 128;
+  const dim3 g2((W + T - 1) / T, H);
+  const unsigned g1 = (unsigned)((N + 255) / 256);
+  cudaStream_t st = q.st;
+  switch (phase) {
+    case OS_PHASE_FORCES:
+      k_forces<S, A><<<g2, T, 0, st>>>(u, v, s, c, h->smoke_period, h->d_params);
+      q.count++;
+      break;
+    case OS_PHASE_ZERO_PRESSURE:
+      k_zero<<<g1, 256, 0, st>>>(h->p, N);
+      q.count++;
+      break;
+    case OS_PHASE_DIFFUSION: {
+      if (h->block_k > 0 && blocked_supported<S, A>(h)) {
+        q.count += enqueue_blocked_diffusion<S, A>(h, st);
+        break;
+      }
+      // Jacobi ping-pong u -> ub -> u ...; an odd count ends with a copy back.
+      for (int t = 0; t < c.n; t++) {
+        const S* in = (t & 1) ? ub : u;
+        S* out = (t & 1) ? u : ub;
+        k_diffuse<S, A><<<g2, T, 0, st>>>(in, out, c, h->d_params);
+        q.count++;
+      }
+      if (c.n & 1) {
+        k_copy1<S><<<g1, 256, 0, st>>>(ub, u, N);
+        q.count++;
+      }
+      break;
+    }
+    case OS_PHASE_PROJECTION: {
+      if (h->block_k > 0 && blocked_supported<S, A>(h)) {
+        q.count += enqueue_blocked_projection<S, A>(h, st);
+        break;
+      }
+      const int half = (W + 1) / 2;
+      const dim3 gp((half + T - 1) / T, H);
+      for (int t = 0; t < c.n; t++) {
+        k_project_half<S, A, 0><<<gp, T, 0, st>>>(u, v, h->p, h->flags, c, h->d_params);
+        k_project_half<S, A, 1><<<gp, T, 0, st>>>(u, v, h->p, h->flags, c, h->d_params);
+        q.count += 2;
+      }
+      break;
+    }
+    case OS_PHASE_PRESSURE_RANGE:
+      k_prange_init<<<1, 32, 0, st>>>(h->d_pkeys);
+      k_prange<<<152 * 4, 256, 0, st>>>(h->p, N, h->d_pkeys);
+      q.count += 2;
+      break;
+    case OS_PHASE_EXTRAPOLATION:
+      k_extrapolate<S><<<1, 1024, 0, st>>>(u, v, c);
+      q.count++;
+      break;
+    case OS_PHASE_VEL_ADVECTION:
+      k_advect_velocity<S, A><<<g2, T, 0, st>>>(u, v, ub, vb, h->flags, c, h->d_params);
+      k_copy2<S><<<g1, 256, 0, st>>>(ub, vb, u, v, N);
+      q.count += 2;
+      break;
+    case OS_PHASE_SMOKE_ADVECTION:
+      // Stand-alone phase: velocities are already in u, v.
+      k_advect_smoke<S, A, false><<<g2, T, 0, st>>>(u, v, s, sb, nullptr, nullptr, h->flags, c, h->d_params);
+      k_copy1<S><<<g1, 256, 0, st>>>(sb, s, N);
+      q.count += 2;
+      break;
+    case OS_PHASE_DECAY: {
+      Consts cc = c;
+      k_finish_smoke<S, A><<<g1, 256, 0, st>>>(s, s, cc, h->d_params, N);
+      q.count++;
+      break;
+    }
+    default:
+      return set_err(OS_ERR_INVALID, "unknown phase %d", phase);
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return set_err(OS_ERR_CUDA, "launch failed: %s", cudaGetErrorString(e));
+  return OS_OK;
+}
+
+// Fluid::update (src/fluid.cu:770-795) as one fused launch sequence.
+template <class S, class A>
+int enqueue_step(os_handle* h, Enq& q) {
+  const os_config& cfg = h->cfg;
+  int rc;
+  if ((rc = enqueue_phase<S, A>(h, OS_PHASE_FORCES, q))) return rc;
+  if (cfg.enable_pressure && (rc = enqueue_phase<S, A>(h, OS_PHASE_ZERO_PRESSURE, q))) return rc;
+  if (cfg.viscosity != 0.0f && (rc = enqueue_phase<S, A>(h, OS_PHASE_DIFFUSION, q))) return rc;
+  if ((rc = enqueue_phase<S, A>(h, OS_PHASE_PROJECTION, q))) return rc;
+  if (cfg.enable_pressure && (rc = enqueue_phase<S, A>(h, OS_PHASE_PRESSURE_RANGE, q))) return rc;
+  if ((rc = enqueue_phase<S, A>(h, OS_PHASE_EXTRAPOLATION, q))) return rc;
+  S* u = static_cast<S*>(h->u);
+  S* v = static_cast<S*>(h->v);
+  S* s = static_cast<S*>(h->s);
+  S* ub = static_cast<S*>(h->ub);
+  S* vb = static_cast<S*>(h->vb);
+  S* sb = static_cast<S*>(h->sb);
+  const int T = 128;
+  const dim3 g2((h->W + T - 1) / T, h->H);
+  const int64_t N = (int64_t)h->N;
+  const unsigned g1 = (unsigned)((N + 255) / 256);
+  k_advect_velocity<S, A><<<g2, T, 0, q.st>>>(u, v, ub, vb, h->flags, h->c, h->d_params);
+  q.count++;
+  if (cfg.enable_smoke && cfg.tunnel_smoke != 0.0f) {
+    // smoke advection on the new velocities, copying them back as it goes
+    k_advect_smoke<S, A, true><<<g2, T, 0, q.st>>>(ub, vb, s, sb, u, v, h->flags, h->c, h->d_params);
+    k_finish_smoke<S, A><<<g1, 256, 0, q.st>>>(sb, s, h->c, h->d_params, N);
+    q.count += 2;
+  } else {
+    k_copy2<S><<<g1, 256, 0, q.st>>>(ub, vb, u, v, N);
+    q.count++;
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return set_err(OS_ERR_CUDA, "launch failed: %s", cudaGetErrorString(e));
+  return OS_OK;
+}
+
+int dispatch_step(os_handle* h, Enq& q) {
+  switch (h->storage) {
+    case OS_STORAGE_F32: return enqueue_step<float, float>(h, q);
+    case OS_STORAGE_F16: return enqueue_step<__half, float>(h, q);
+    case OS_STORAGE_BF16: return enqueue_step<__nv_bfloat16, float>(h, q);
+    case OS_STORAGE_F64: return enqueue_step<double, double>(h, q);
+  }
+  return set_err(OS_ERR_INVALID, "bad storage");
+}
+
+int dispatch_phase(os_handle* h, int phase, Enq& q) {
+  switch (h->storage) {
+    case OS_STORAGE_F32: return enqueue_phase<float, float>(h, phase, q);
+    case OS_STORAGE_F16: return enqueue_phase<__half, float>(h, phase, q);
+    case OS_STORAGE_BF16: return enqueue_phase<__nv_bfloat16, float>(h, phase, q);
+    case OS_STORAGE_F64: return enqueue_phase<double, double>(h, phase, q);
+  }
+  return set_err(OS_ERR_INVALID, "bad storage");
+}
+
+int build_graph(os_handle* h) {
+  if (h->graph) return OS_OK;
+  Enq q{h->stream};
+  CUDA_OR_RETURN(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  int rc = dispatch_step(h, q);
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+  if (rc) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (e != cudaSuccess) return set_err(OS_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+  e = cudaGraphInstantiate(&h->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return set_err(OS_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+  h->kernels_per_step = q.count;
+  return OS_OK;
+}
+
+int push_params(os_handle* h, const os_source* src, float dt, cudaStream_t st) {
+  StepParams p;
+  memset(&p, 0, sizeof p);
+  p.dt = dt;
+  if (src && src->active) {
+    p.src_active = 1;
+    p.src_smoke = src->smoke;
+    p.src_velocity = src->velocity;
+    p.src_x = src->position_x;
+    p.src_y = src->position_y;
+  }
+  if (h->params_valid && memcmp(&p, &h->last_params, sizeof p) == 0) return OS_OK;
+  // Pinned staging slot; the previous copy out of it must have completed
+  // before it is rewritten.
+  CUDA_OR_RETURN(cudaEventSynchronize(h->params_event));
+  *h->h_params = p;
+  CUDA_OR_RETURN(cudaMemcpyAsync(h->d_params, h->h_params, sizeof p, cudaMemcpyHostToDevice, st));
+  CUDA_OR_RETURN(cudaEventRecord(h->params_event, st));
+  h->params_bytes += sizeof p;
+  h->last_params = p;
+  h->params_valid = true;
+  return OS_OK;
+}
+
+int validate(const os_config* c) {
+  if (c->width < 3 || c->height < 3)
+    return set_err(OS_ERR_INVALID, "grid must be at least 3x3 (got %dx%d)", c->width, c->height);
+  if ((int64_t)c->width * c->height > (int64_t)1 << 34)
+    return set_err(OS_ERR_INVALID, "grid too large");
+  if ((int)c->cell_size < 1)
+    return set_err(OS_ERR_INVALID, "sim.cell_size must be >= 1 (Fluid truncates it to int)");
+  if (c->projection_n < 0) return set_err(OS_ERR_INVALID, "sim.projection.n must be >= 0");
+  if (c->block_size_x < 1 || c->block_size_y < 1)
+    return set_err(OS_ERR_INVALID, "thread.cuda.block_size_* must be >= 1");
+  if (storage_bytes(c->storage) == 0) return set_err(OS_ERR_INVALID, "unknown storage %d", c->storage);
+  if (c->smoke_count != 1) {
+    if (c->smoke_count - 1 == 0) return set_err(OS_ERR_INVALID, "smoke_count");
+    const int spacing = (c->pipe_height - c->smoke_count * c->smoke_height) / (c->smoke_count - 1);
+    if (spacing + c->smoke_height == 0)
+      return set_err(OS_ERR_INVALID,
+                     "sim.wind_tunnel.smoke_count/smoke_height give a zero smoke period");
+  }
+  return OS_OK;
+}
+
+void free_handle(os_handle* h) {
+  if (!h) return;
+  if (h->graph) cudaGraphExecDestroy(h->graph);
+  void* ptrs[] = {h->u, h->v, h->s, h->ub, h->vb, h->sb, h->p, h->is_solid,
+                  h->total_s, h->flags, h->d_params, h->d_pkeys, h->conv};
+  for (void* q : ptrs)
+    if (q) cudaFree(q);
+  if (h->h_pkeys) cudaFreeHost(h->h_pkeys);
+  if (h->h_params) cudaFreeHost(h->h_params);
+  if (h->params_event) cudaEventDestroy(h->params_event);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+}
+
+int select_device(const os_handle* h) {
+  int cur = -1;
+  CUDA_OR_RETURN(cudaGetDevice(&cur));
+  if (cur != h->cfg.device) CUDA_OR_RETURN(cudaSetDevice(h->cfg.device));
+  return OS_OK;
+}
+
+// Host-side float <-> storage conversions for os_upload/os_download.
+template <class S>
+__global__ void k_from_f32(const float* __restrict__ a, S* __restrict__ x, int64_t n) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) st(x + k, a[k]);
+}
+template <>
+__global__ void k_from_f32<double>(const float* __restrict__ a, double* __restrict__ x, int64_t n) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) x[k] = (double)a[k];
+}
+template <class S>
+__global__ void k_to_f32(const S* __restrict__ x, float* __restrict__ a, int64_t n) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) a[k] = (float)ld<float, S>(x + k);
+}
+template <>
+__global__ void k_to_f32<double>(const double* __restrict__ x, float* __restrict__ a, int64_t n) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) a[k] = (float)x[k];
+}
+
+int convert(os_handle* h, void* field, bool to_storage) {
+  const int64_t N = (int64_t)h->N;
+  const unsigned g = (unsigned)((N + 255) / 256);
+  switch (h->storage) {
+    case OS_STORAGE_F16:
+      if (to_storage) k_from_f32<__half><<<g, 256, 0, h->stream>>>(h->conv, (__half*)field, N);
+      else k_to_f32<__half><<<g, 256, 0, h->stream>>>((const __half*)field, h->conv, N);
+      break;
+    case OS_STORAGE_BF16:
+      if (to_storage) k_from_f32<__nv_bfloat16><<<g, 256, 0, h->stream>>>(h->conv, (__nv_bfloat16*)field, N);
+      else k_to_f32<__nv_bfloat16><<<g, 256, 0, h->stream>>>((const __nv_bfloat16*)field, h->conv, N);
+      break;
+    case OS_STORAGE_F64:
+      if (to_storage) k_from_f32<double><<<g, 256, 0, h->stream>>>(h->conv, (double*)field, N);
+      else k_to_f32<double><<<g, 256, 0, h->stream>>>((const double*)field, h->conv, N);
+      break;
+    default:
+      return set_err(OS_ERR_INVALID, "bad storage");
+  }
+  h->launches++;
+  CUDA_OR_RETURN(cudaGetLastError());
+  return OS_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+
+extern "C" {
+
+int32_t os_abi_version(void) { return OS_ABI_VERSION; }
+
+const char* os_last_error(void) { return g_err; }
+
+int os_config_defaults(int32_t width, int32_t height, os_config* out) {
+  if (!out) return set_err(OS_ERR_INVALID, "null config");
+  if (width < 1 || height < 1) return set_err(OS_ERR_INVALID, "bad size");
+  memset(out, 0, sizeof *out);
+  // src/config_parser.cpp:21-179, in order.
+  out->block_size_x = 64;
+  out->block_size_y = 1;
+  out->height = height;
+  out->width = width;
+  out->cell_pixel_size = 1;
+  out->cell_size = 1.0f;
+  out->enable_drain = 1;
+  out->enable_pressure = 0;
+  out->enable_smoke = 1;
+  out->enable_interactive = 0;
+  out->projection_n = 50;
+  out->projection_o = 1.9f;
+  out->pipe_height = height / 4;
+  out->pipe_length = 0;  // hard-coded by the parser (config_parser.cpp:64)
+  out->smoke_length = 1;
+  out->smoke_height = height / 4;
+  out->smoke_count = 1;
+  out->tunnel_speed = 0.0f;
+  out->tunnel_smoke = 1.0f;
+  out->g = 0.0f;
+  out->d_t = 0.05f;
+  out->enable_real_time = 0;
+  out->real_time_multiplier = 1.0f;
+  out->smoke_enable_decay = 0;
+  out->smoke_decay_rate = 0.05f;
+  out->obstacle_enable = 1;
+  out->obstacle_center_x = width / 2;
+  out->obstacle_center_y = height / 2;
+  out->obstacle_radius = std::min(height, width) / 30.0f;
+  out->density = 1.0f;
+  out->drag_coeff = 0.0f;
+  out->viscosity = 0.001f;
+  out->storage = OS_STORAGE_F32;
+  out->device = 0;
+  out->projection_block = 0;
+  out->fast_idw = 0;
+  return OS_OK;
+}
+
+int os_create(const os_config* cfg, os_handle** out) {
+  if (!cfg || !out) return set_err(OS_ERR_INVALID, "null argument");
+  *out = nullptr;
+  int rc = validate(cfg);
+  if (rc) return rc;
+  os_handle* h = new (std::nothrow) os_handle();
+  if (!h) return set_err(OS_ERR_NOMEM, "host allocation failed");
+  h->cfg = *cfg;
+  h->W = cfg->width;
+  h->H = cfg->height;
+  h->N = (size_t)cfg->width * cfg->height;
+  h->storage = cfg->storage;
+  h->esize = storage_bytes(cfg->storage);
+  Consts& c = h->c;
+  c.W = cfg->width;
+  c.H = cfg->height;
+  c.h = (int)cfg->cell_size;
+  c.n = cfg->projection_n;
+  c.g = cfg->g;
+  c.density = cfg->density;
+  c.viscosity = cfg->viscosity;
+  c.o = cfg->projection_o;
+  c.drag = cfg->drag_coeff;
+  c.speed = cfg->tunnel_speed;
+  c.tunnel_smoke = cfg->tunnel_smoke;
+  c.decay_rate = cfg->smoke_decay_rate;
+  c.smoke_length = cfg->smoke_length;
+  c.smoke_count = cfg->smoke_count;
+  c.smoke_height = cfg->smoke_height;
+  c.pipe_height = cfg->pipe_height;
+  c.enable_decay = cfg->smoke_enable_decay != 0;
+  c.enable_pressure = cfg->enable_pressure != 0;
+  c.fast_idw = cfg->fast_idw != 0;
+  if (cfg->smoke_count != 1) {
+    const int spacing = (cfg->pipe_height - cfg->smoke_count * cfg->smoke_height) /
+                        (cfg->smoke_count - 1);
+    h->smoke_period = spacing + cfg->smoke_height;
+  }
+  h->block_k = choose_block_k(h);
+
+  auto fail = [&](int code) {
+    free_handle(h);
+    return code;
+  };
+  cudaError_t e = cudaSetDevice(cfg->device);
+  if (e != cudaSuccess)
+    return fail(set_err(OS_ERR_CUDA, "cudaSetDevice(%d): %s", cfg->device, cudaGetErrorString(e)));
+  if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess)
+    return fail(set_err(OS_ERR_CUDA, "stream: %s", cudaGetErrorString(e)));
+  const size_t fb = h->N * h->esize;
+  void** fields[] = {&h->u, &h->v, &h->s, &h->ub, &h->vb, &h->sb};
+  for (void** f : fields) {
+    if ((e = cudaMalloc(f, fb)) != cudaSuccess)
+      return fail(set_err(OS_ERR_NOMEM, "cudaMalloc(%zu): %s", fb, cudaGetErrorString(e)));
+    cudaMemsetAsync(*f, 0, fb, h->stream);
+  }
+  if ((e = cudaMalloc(&h->p, h->N * 4)) != cudaSuccess ||
+      (e = cudaMalloc(&h->is_solid, h->N * 4)) != cudaSuccess ||
+      (e = cudaMalloc(&h->total_s, h->N * 4)) != cudaSuccess ||
+      (e = cudaMalloc(&h->flags, h->N)) != cudaSuccess ||
+      (e = cudaMalloc(&h->d_params, sizeof(StepParams))) != cudaSuccess ||
+      (e = cudaMalloc(&h->d_pkeys, 2 * sizeof(int))) != cudaSuccess)
+    return fail(set_err(OS_ERR_NOMEM, "cudaMalloc: %s", cudaGetErrorString(e)));
+  if ((e = cudaMallocHost(&h->h_pkeys, 2 * sizeof(int))) != cudaSuccess ||
+      (e = cudaMallocHost(&h->h_params, sizeof(StepParams))) != cudaSuccess)
+    return fail(set_err(OS_ERR_NOMEM, "cudaMallocHost: %s", cudaGetErrorString(e)));
+  if ((e = cudaEventCreateWithFlags(&h->params_event, cudaEventDisableTiming)) != cudaSuccess)
+    return fail(set_err(OS_ERR_CUDA, "event: %s", cudaGetErrorString(e)));
+  cudaMemsetAsync(h->p, 0, h->N * 4, h->stream);
+  MaskParams m;
+  m.enable_drain = cfg->enable_drain != 0;
+  m.obstacle_enable = cfg->obstacle_enable != 0;
+  m.cx = cfg->obstacle_center_x;
+  m.cy = cfg->obstacle_center_y;
+  m.pipe_length = cfg->pipe_length;
+  m.pipe_height = cfg->pipe_height;
+  m.radius = cfg->obstacle_radius;
+  const dim3 g2((h->W + 127) / 128, h->H);
+  k_init_solid<<<g2, 128, 0, h->stream>>>(h->is_solid, c, m);
+  k_init_flags<<<g2, 128, 0, h->stream>>>(h->is_solid, h->total_s, h->flags, c);
+  h->launches += 2;
+  if ((e = cudaGetLastError()) != cudaSuccess ||
+      (e = cudaStreamSynchronize(h->stream)) != cudaSuccess)
+    return fail(set_err(OS_ERR_CUDA, "init: %s", cudaGetErrorString(e)));
+  *out = h;
+  return OS_OK;
+}
+
+int os_destroy(os_handle* h) {
+  if (!h) return OS_OK;
+  cudaSetDevice(h->cfg.device);
+  cudaStreamSynchronize(h->stream);
+  free_handle(h);
+  return OS_OK;
+}
+
+int os_update_async(os_handle* h, const os_source* src, float dt, int32_t steps, void* stream) {
+  if (!h) return set_err(OS_ERR_INVALID, "null handle");
+  if (steps < 0) return set_err(OS_ERR_INVALID, "steps < 0");
+  int rc = select_device(h);
+  if (rc) return rc;
+  if ((rc = build_graph(h))) return rc;
+  cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : h->stream;
+  if ((rc = push_params(h, src, dt, st))) return rc;
+  for (int t = 0; t < steps; t++) CUDA_OR_RETURN(cudaGraphLaunch(h->graph, st));
+  h->launches += (int64_t)steps * h->kernels_per_step;
+  return OS_OK;
+}
+
+int os_synchronize(os_handle* h) {
+  if (!h) return set_err(OS_ERR_INVALID, "null handle");
+  CUDA_OR_RETURN(cudaStreamSynchronize(h->stream));
+  return OS_OK;
+}
+
+int os_update(os_handle* h, const os_source* src, float dt) {
+  int rc = os_update_async(h, src, dt, 1, nullptr);
+  if (rc) return rc;
+  if (h->cfg.enable_pressure)
+    CUDA_OR_RETURN(cudaMemcpyAsync(h->h_pkeys, h->d_pkeys, 2 * sizeof(int),
+                                   cudaMemcpyDeviceToHost, h->stream));
+  CUDA_OR_RETURN(cudaStreamSynchronize(h->stream));
+  if (h->cfg.enable_pressure) {
+    h->min_pressure = key_to_float(h->h_pkeys[0]);
+    h->max_pressure = key_to_float(h->h_pkeys[1]);
+  }
+  return OS_OK;
+}
+
+int os_fields(os_handle* h, os_fields_view* out) {
+  if (!h || !out) return set_err(OS_ERR_INVALID, "null argument");
+  memset(out, 0, sizeof *out);
+  out->width = h->W;
+  out->height = h->H;
+  out->storage = h->storage;
+  out->vel_x = h->u;
+  out->vel_y = h->v;
+  out->smoke = h->s;
+  out->pressure = h->p;
+  out->is_solid = h->is_solid;
+  out->total_s = h->total_s;
+  return OS_OK;
+}
+
+static int field_target(os_handle* h, int32_t field, void** ptr, bool* is_float_field) {
+  *is_float_field = true;
+  switch (field) {
+    case OS_FIELD_VEL_X: *ptr = h->u; return OS_OK;
+    case OS_FIELD_VEL_Y: *ptr = h->v; return OS_OK;
+    case OS_FIELD_SMOKE: *ptr = h->s; return OS_OK;
+    case OS_FIELD_PRESSURE: *ptr = h->p; *is_float_field = false; return OS_OK;
+    case OS_FIELD_IS_SOLID: *ptr = h->is_solid; *is_float_field = false; return OS_OK;
+    case OS_FIELD_TOTAL_S: *ptr = h->total_s; *is_float_field = false; return OS_OK;
+  }
+  return set_err(OS_ERR_INVALID, "unknown field %d", field);
+}
+
+int os_upload(os_handle* h, int32_t field, const void* host, size_t count) {
+  if (!h || !host) return set_err(OS_ERR_INVALID, "null argument");
+  if (count != h->N) return set_err(OS_ERR_INVALID, "count %zu != width*height %zu", count, h->N);
+  if (field == OS_FIELD_IS_SOLID || field == OS_FIELD_TOTAL_S)
+    return set_err(OS_ERR_INVALID, "the solid mask and neighbour counts are fixed at creation");
+  void* dst;
+  bool storage_field;
+  int rc = field_target(h, field, &dst, &storage_field);
+  if (rc) return rc;
+  if ((rc = select_device(h))) return rc;
+  if (!storage_field || h->storage == OS_STORAGE_F32) {
+    CUDA_OR_RETURN(cudaMemcpyAsync(dst, host, h->N * 4, cudaMemcpyHostToDevice, h->stream));
+  } else {
+    if (!h->conv) CUDA_OR_RETURN(cudaMalloc(&h->conv, h->N * 4));
+    CUDA_OR_RETURN(cudaMemcpyAsync(h->conv, host, h->N * 4, cudaMemcpyHostToDevice, h->stream));
+    if ((rc = convert(h, dst, true))) return rc;
+  }
+  CUDA_OR_RETURN(cudaStreamSynchronize(h->stream));
+  return OS_OK;
+}
+
+int os_download(os_handle* h, int32_t field, void* host, size_t count) {
+  if (!h || !host) return set_err(OS_ERR_INVALID, "null argument");
+  if (count != h->N) return set_err(OS_ERR_INVALID, "count %zu != width*height %zu", count, h->N);
+  void* src;
+  bool storage_field;
+  int rc = field_target(h, field, &src, &storage_field);
+  if (rc) return rc;
+  if ((rc = select_device(h))) return rc;
+  if (!storage_field || h->storage == OS_STORAGE_F32) {
+    CUDA_OR_RETURN(cudaMemcpyAsync(host, src, h->N * 4, cudaMemcpyDeviceToHost, h->stream));
+  } else {
+    if (!h->conv) CUDA_OR_RETURN(cudaMalloc(&h->conv, h->N * 4));
+    if ((rc = convert(h, src, false))) return rc;
+    CUDA_OR_RETURN(cudaMemcpyAsync(host, h->conv, h->N * 4, cudaMemcpyDeviceToHost, h->stream));
+  }
+  CUDA_OR_RETURN(cudaStreamSynchronize(h->stream));
+  return OS_OK;
+}
+
+int os_pressure_range(os_handle* h, float* min_out, float* max_out) {
+  if (!h || !min_out || !max_out) return set_err(OS_ERR_INVALID, "null argument");
+  *min_out = h->min_pressure;
+  *max_out = h->max_pressure;
+  return OS_OK;
+}
+
+int os_run_phase(os_handle* h, int32_t phase, const os_source* src, float dt) {
+  if (!h) return set_err(OS_ERR_INVALID, "null handle");
+  int rc = select_device(h);
+  if (rc) return rc;
+  if ((rc = push_params(h, src, dt, h->stream))) return rc;
+  Enq q{h->stream};
+  if ((rc = dispatch_phase(h, phase, q))) return rc;
+  h->launches += q.count;
+  if (phase == OS_PHASE_PRESSURE_RANGE)
+    CUDA_OR_RETURN(cudaMemcpyAsync(h->h_pkeys, h->d_pkeys, 2 * sizeof(int),
+                                   cudaMemcpyDeviceToHost, h->stream));
+  CUDA_OR_RETURN(cudaStreamSynchronize(h->stream));
+  if (phase == OS_PHASE_PRESSURE_RANGE) {
+    h->min_pressure = key_to_float(h->h_pkeys[0]);
+    h->max_pressure = key_to_float(h->h_pkeys[1]);
+  }
+  return OS_OK;
+}
+
+int os_kernel_launches(os_handle* h, int64_t* out) {
+  if (!h || !out) return set_err(OS_ERR_INVALID, "null argument");
+  *out = h->launches;
+  return OS_OK;
+}
+
+int os_profile_phase(os_handle* h, int32_t phase, const os_source* src, float dt, int32_t reps,
+                     void* stream, float* ms_out, int32_t* kernels_out) {
+  if (!h || !ms_out || reps < 1) return set_err(OS_ERR_INVALID, "bad argument");
+  int rc = select_device(h);
+  if (rc) return rc;
+  cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : h->stream;
+  if ((rc = push_params(h, src, dt, st))) return rc;
+  cudaEvent_t a = nullptr, b = nullptr;
+  CUDA_OR_RETURN(cudaEventCreate(&a));
+  CUDA_OR_RETURN(cudaEventCreate(&b));
+  Enq q{st};
+  cudaEventRecord(a, st);
+  for (int r = 0; r < reps && rc == OS_OK; r++) rc = dispatch_phase(h, phase, q);
+  cudaEventRecord(b, st);
+  cudaError_t e = cudaEventSynchronize(b);
+  float ms = 0.0f;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (rc) return rc;
+  if (e != cudaSuccess) return set_err(OS_ERR_CUDA, "profile: %s", cudaGetErrorString(e));
+  h->launches += q.count;
+  *ms_out = ms;
+  if (kernels_out) *kernels_out = q.count;
+  return OS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,245 @@
+"""Python mirror of the reference's simulation interface.
+
+`Fluid(config)` / `Fluid.update(source, d_t)` follow the reference's class
+`Fluid` (inc/fluid.cuh:15-116, src/fluid.cu:41-71,770-795); `Source` follows
+inc/fluid.cuh:8-13; `load_config` follows ConfigParser (inc/config_parser.hpp:
+131-150, src/config_parser.cpp:15-184). Every call goes through the C ABI of
+libopensayal_gb300.so; the arithmetic runs on the GPU only.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import json
+from dataclasses import dataclass
+from pathlib import Path
+from typing import Any
+
+import numpy as np
+
+from . import native
+from .native import OsConfig, OsFieldsView, OsSource, check
+
+
+@dataclass
+class Source:
+    """The reference's Source: an interactive forcing disc of radius 40 cells."""
+
+    active: bool = False
+    smoke: float = 0.0
+    velocity: float = 0.0
+    position: tuple[int, int] = (0, 0)
+
+    def to_native(self) -> OsSource:
+        return OsSource(int(bool(self.active)), float(self.smoke), float(self.velocity),
+                        int(self.position[0]), int(self.position[1]))
+
+
+def default_config(width: int = 1920, height: int = 1080) -> OsConfig:
+    """ConfigParser defaults for a width x height tunnel (src/config_parser.cpp:21-179)."""
+    cfg = OsConfig()
+    check(native.load().os_config_defaults(width, height, C.byref(cfg)))
+    return cfg
+
+
+# Reference config key -> (os_config field, type). src/config_parser.cpp:21-179.
+CONFIG_KEYS: dict[str, tuple[str, type]] = {
+    "thread.cuda.block_size_x": ("block_size_x", int),
+    "thread.cuda.block_size_y": ("block_size_y", int),
+    "sim.height": ("height", int),
+    "sim.width": ("width", int),
+    "sim.cell_pixel_size": ("cell_pixel_size", int),
+    "sim.cell_size": ("cell_size", float),
+    "sim.enable_drain": ("enable_drain", bool),
+    "sim.enable_pressure": ("enable_pressure", bool),
+    "sim.enable_smoke": ("enable_smoke", bool),
+    "sim.enable_interactive": ("enable_interactive", bool),
+    "sim.projection.n": ("projection_n", int),
+    "sim.projection.o": ("projection_o", float),
+    "sim.wind_tunnel.pipe_height": ("pipe_height", int),
+    "sim.wind_tunnel.smoke_length": ("smoke_length", int),
+    "sim.wind_tunnel.smoke_height": ("smoke_height", int),
+    "sim.wind_tunnel.smoke_count": ("smoke_count", int),
+    "sim.wind_tunnel.speed": ("tunnel_speed", float),
+    "sim.wind_tunnel.smoke": ("tunnel_smoke", float),
+    "sim.physics.g": ("g", float),
+    "sim.time.d_t": ("d_t", float),
+    "sim.time.enable_real_time": ("enable_real_time", bool),
+    "sim.time.real_time_multiplier": ("real_time_multiplier", float),
+    "sim.smoke.enable_decay": ("smoke_enable_decay", bool),
+    "sim.smoke.decay_rate": ("smoke_decay_rate", float),
+    "sim.obstacle.enable": ("obstacle_enable", bool),
+    "sim.obstacle.center_x": ("obstacle_center_x", int),
+    "sim.obstacle.center_y": ("obstacle_center_y", int),
+    "sim.obstacle.radius": ("obstacle_radius", float),
+    "fluid.density": ("density", float),
+    "fluid.drag_coeff": ("drag_coeff", float),
+    "fluid.viscosity": ("viscosity", float),
+}
+
+_MISSING = object()
+
+
+def _get_or(obj: Any, key: str) -> Any:
+    """ConfigParser::get_or (inc/config_parser.hpp:131-150): the whole dotted key
+    at this level first, then recurse on the part before the first dot."""
+    if isinstance(obj, dict) and key in obj:
+        return obj[key]
+    if key == "" or "." not in key:
+        return _MISSING
+    parent, child = key.split(".", 1)
+    if not isinstance(obj, dict) or parent not in obj:
+        return _MISSING
+    return _get_or(obj[parent], child)
+
+
+def _convert(value: Any, typ: type, key: str) -> Any:
+    if typ is bool:
+        if not isinstance(value, bool):
+            raise TypeError(f"config key {key!r} must be a boolean, got {value!r}")
+        return int(value)
+    if isinstance(value, bool) or not isinstance(value, (int, float)):
+        raise TypeError(f"config key {key!r} must be a number, got {value!r}")
+    return int(value) if typ is int else float(value)
+
+
+def load_config(source: dict | str | Path) -> OsConfig:
+    """Parse an OpenSayal.conf.json (path, JSON text or dict) with the reference's
+    defaults and dotted-key lookup. Size-dependent defaults (pipe and smoke
+    heights, obstacle centre and radius) follow the parsed width and height."""
+    if isinstance(source, dict):
+        obj = source
+    else:
+        text = Path(source).read_text() if Path(str(source)).exists() else str(source)
+        obj = json.loads(text)
+    width = _get_or(obj, "sim.width")
+    height = _get_or(obj, "sim.height")
+    width = 1920 if width is _MISSING else _convert(width, int, "sim.width")
+    height = 1080 if height is _MISSING else _convert(height, int, "sim.height")
+    cfg = default_config(width, height)
+    for key, (field, typ) in CONFIG_KEYS.items():
+        val = _get_or(obj, key)
+        if val is not _MISSING:
+            setattr(cfg, field, _convert(val, typ, key))
+    return cfg
+
+
+FIELD_IDS = {
+    "vel_x": native.FIELD_VEL_X,
+    "vel_y": native.FIELD_VEL_Y,
+    "smoke": native.FIELD_SMOKE,
+    "pressure": native.FIELD_PRESSURE,
+    "is_solid": native.FIELD_IS_SOLID,
+    "total_s": native.FIELD_TOTAL_S,
+}
+
+
+class Fluid:
+    """The reference's Fluid on the GB300 library. Fields stay in device memory
+    in the reference layout indx(i, j) = (height - 1 - j) * width + i."""
+
+    def __init__(self, config: OsConfig):
+        self._lib = native.load()
+        self.config = config.copy()
+        h = C.c_void_p()
+        check(self._lib.os_create(C.byref(self.config), C.byref(h)))
+        self._h = h
+        self.width = config.width
+        self.height = config.height
+        self.n = config.projection_n
+        self.o = config.projection_o
+        self.cell_size = int(config.cell_size)
+
+    # -- lifecycle -----------------------------------------------------------
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            check(self._lib.os_destroy(self._h))
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- the step ------------------------------------------------------------
+    def update(self, source: Source | None, d_t: float) -> None:
+        """Fluid::update(Source, float): one synchronous step."""
+        src = (source or Source()).to_native()
+        check(self._lib.os_update(self._h, C.byref(src), C.c_float(d_t)))
+
+    def update_async(self, source: Source | None, d_t: float, steps: int = 1,
+                     stream: int | None = None) -> None:
+        """`steps` graph replays on `stream` (a cudaStream_t value) without waiting."""
+        src = (source or Source()).to_native()
+        check(self._lib.os_update_async(self._h, C.byref(src), C.c_float(d_t), int(steps),
+                                        C.c_void_p(stream) if stream else None))
+
+    def synchronize(self) -> None:
+        check(self._lib.os_synchronize(self._h))
+
+    def run_phase(self, phase: int, source: Source | None, d_t: float) -> None:
+        src = (source or Source()).to_native()
+        check(self._lib.os_run_phase(self._h, int(phase), C.byref(src), C.c_float(d_t)))
+
+    def profile_phase(self, phase: int, source: Source | None, d_t: float, reps: int,
+                      stream: int | None = None) -> tuple[float, int]:
+        """(milliseconds, kernels) for `reps` repetitions of one phase, timed with
+        CUDA events on the stream the kernels run on."""
+        src = (source or Source()).to_native()
+        ms, kern = C.c_float(), C.c_int32()
+        check(self._lib.os_profile_phase(self._h, int(phase), C.byref(src), C.c_float(d_t),
+                                         int(reps), C.c_void_p(stream) if stream else None,
+                                         C.byref(ms), C.byref(kern)))
+        return ms.value, kern.value
+
+    # -- state ---------------------------------------------------------------
+    def indx(self, i: int, j: int) -> int:
+        return (self.height - j - 1) * self.width + i
+
+    def fields(self) -> OsFieldsView:
+        view = OsFieldsView()
+        check(self._lib.os_fields(self._h, C.byref(view)))
+        return view
+
+    def download(self, field: str | int, out: np.ndarray | None = None) -> np.ndarray:
+        fid = FIELD_IDS[field] if isinstance(field, str) else field
+        dtype = np.int32 if fid in (native.FIELD_IS_SOLID, native.FIELD_TOTAL_S) else np.float32
+        n = self.width * self.height
+        if out is None:
+            out = np.empty(n, dtype=dtype)
+        assert out.dtype == dtype and out.size == n and out.flags.c_contiguous
+        check(self._lib.os_download(self._h, fid, out.ctypes.data_as(C.c_void_p), n))
+        return out
+
+    def upload(self, field: str | int, data: np.ndarray) -> None:
+        fid = FIELD_IDS[field] if isinstance(field, str) else field
+        arr = np.ascontiguousarray(data, dtype=np.float32).reshape(-1)
+        check(self._lib.os_upload(self._h, fid, arr.ctypes.data_as(C.c_void_p), arr.size))
+
+    @property
+    def min_pressure(self) -> float:
+        lo, hi = C.c_float(), C.c_float()
+        check(self._lib.os_pressure_range(self._h, C.byref(lo), C.byref(hi)))
+        return lo.value
+
+    @property
+    def max_pressure(self) -> float:
+        lo, hi = C.c_float(), C.c_float()
+        check(self._lib.os_pressure_range(self._h, C.byref(lo), C.byref(hi)))
+        return hi.value
+
+    @property
+    def kernel_launches(self) -> int:
+        out = C.c_int64()
+        check(self._lib.os_kernel_launches(self._h, C.byref(out)))
+        return out.value
+
+    @property
+    def handle(self) -> int:
+        return self._h.value
