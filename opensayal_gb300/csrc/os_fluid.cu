@@ -100,88 +100,151 @@ struct Enq {
   int count = 0;
 };
 
+// Where the live velocity sits while a step is enqueued: 0 = the public
+// fields u/v, 1 = the buffers ub/vb. Blocked passes and advection alternate
+// between the two instead of copying back.
+template <class S>
+struct Vel {
+  S* U[2];
+  S* V[2];
+  int cu = 0, cv = 0;
+  S* u() const { return U[cu]; }
+  S* v() const { return V[cv]; }
+};
+
+template <class S>
+Vel<S> vel_of(os_handle* h) {
+  Vel<S> w;
+  w.U[0] = static_cast<S*>(h->u);
+  w.U[1] = static_cast<S*>(h->ub);
+  w.V[0] = static_cast<S*>(h->v);
+  w.V[1] = static_cast<S*>(h->vb);
+  return w;
+}
+
+template <class S, class A>
+bool use_blocked(const os_handle* h) {
+  return h->block_k > 0 && blocked_supported<S, A>(h);
+}
+
+template <class S, class A>
+void enqueue_diffusion(os_handle* h, Vel<S>& w, Enq& q) {
+  if (use_blocked<S, A>(h)) {
+    q.count += enqueue_blocked_diffusion_f32(h, q.st, &w.cu);
+    return;
+  }
+  const dim3 g2((h->W + 127) / 128, h->H);
+  for (int t = 0; t < h->c.n; t++) {
+    k_diffuse<S, A><<<g2, 128, 0, q.st>>>(w.U[w.cu], w.U[1 - w.cu], h->c, h->d_params);
+    w.cu = 1 - w.cu;
+    q.count++;
+  }
+}
+
+template <class S, class A>
+void enqueue_projection(os_handle* h, Vel<S>& w, Enq& q, bool zero_pressure_first) {
+  if (use_blocked<S, A>(h)) {
+    q.count += enqueue_blocked_projection_f32(h, q.st, &w.cu, &w.cv, zero_pressure_first);
+    return;
+  }
+  const dim3 gp(((h->W + 1) / 2 + 127) / 128, h->H);
+  for (int t = 0; t < h->c.n; t++) {
+    k_project_half<S, A, 0><<<gp, 128, 0, q.st>>>(w.u(), w.v(), h->p, h->flags, h->c, h->d_params);
+    k_project_half<S, A, 1><<<gp, 128, 0, q.st>>>(w.u(), w.v(), h->p, h->flags, h->c, h->d_params);
+    q.count += 2;
+  }
+}
+
+// Copies a field that ended in its buffer back to the public array.
+template <class S>
+void settle(os_handle* h, Vel<S>& w, Enq& q) {
+  const int64_t N = (int64_t)h->N;
+  const unsigned g1 = (unsigned)((N + 255) / 256);
+  if (w.cu) {
+    k_copy1<S><<<g1, 256, 0, q.st>>>(w.U[1], w.U[0], N);
+    q.count++;
+    w.cu = 0;
+  }
+  if (w.cv) {
+    k_copy1<S><<<g1, 256, 0, q.st>>>(w.V[1], w.V[0], N);
+    q.count++;
+    w.cv = 0;
+  }
+}
+
+template <class S, class A>
+void enqueue_smoke_advection(os_handle* h, Vel<S>& w, Enq& q) {
+  S* s = static_cast<S*>(h->s);
+  S* sb = static_cast<S*>(h->sb);
+  S* u0 = w.U[0];
+  S* v0 = w.V[0];
+  const dim3 g2((h->W + 127) / 128, h->H);
+  const Consts& c = h->c;
+  // smoke advection on the live velocities, copying them back as it goes
+  if (w.cu && w.cv)
+    k_advect_smoke<S, A, true, true><<<g2, 128, 0, q.st>>>(w.u(), w.v(), s, sb, u0, v0, h->flags, c, h->d_params);
+  else if (w.cu)
+    k_advect_smoke<S, A, true, false><<<g2, 128, 0, q.st>>>(w.u(), w.v(), s, sb, u0, v0, h->flags, c, h->d_params);
+  else if (w.cv)
+    k_advect_smoke<S, A, false, true><<<g2, 128, 0, q.st>>>(w.u(), w.v(), s, sb, u0, v0, h->flags, c, h->d_params);
+  else
+    k_advect_smoke<S, A, false, false><<<g2, 128, 0, q.st>>>(w.u(), w.v(), s, sb, u0, v0, h->flags, c, h->d_params);
+  w.cu = w.cv = 0;
+  q.count++;
+}
+
 template <class S, class A>
 int enqueue_phase(os_handle* h, int phase, Enq& q) {
   const Consts& c = h->c;
-  S* u = static_cast<S*>(h->u);
-  S* v = static_cast<S*>(h->v);
+  Vel<S> w = vel_of<S>(h);
   S* s = static_cast<S*>(h->s);
-  S* ub = static_cast<S*>(h->ub);
-  S* vb = static_cast<S*>(h->vb);
   S* sb = static_cast<S*>(h->sb);
   const int W = h->W, H = h->H;
   const int64_t N = (int64_t)h->N;
-  const int T = 128;
-  const dim3 g2((W + T - 1) / T, H);
+  const dim3 g2((W + 127) / 128, H);
   const unsigned g1 = (unsigned)((N + 255) / 256);
   cudaStream_t st = q.st;
   switch (phase) {
     case OS_PHASE_FORCES:
-      k_forces<S, A><<<g2, T, 0, st>>>(u, v, s, c, h->smoke_period, h->d_params);
+      k_forces<S, A><<<g2, 128, 0, st>>>(w.u(), w.v(), s, c, h->smoke_period, h->d_params);
       q.count++;
       break;
     case OS_PHASE_ZERO_PRESSURE:
       k_zero<<<g1, 256, 0, st>>>(h->p, N);
       q.count++;
       break;
-    case OS_PHASE_DIFFUSION: {
-      if (h->block_k > 0 && blocked_supported<S, A>(h)) {
-        q.count += enqueue_blocked_diffusion<S, A>(h, st);
-        break;
-      }
-      // Jacobi ping-pong u -> ub -> u ...; an odd count ends with a copy back.
-      for (int t = 0; t < c.n; t++) {
-        const S* in = (t & 1) ? ub : u;
-        S* out = (t & 1) ? u : ub;
-        k_diffuse<S, A><<<g2, T, 0, st>>>(in, out, c, h->d_params);
-        q.count++;
-      }
-      if (c.n & 1) {
-        k_copy1<S><<<g1, 256, 0, st>>>(ub, u, N);
-        q.count++;
-      }
+    case OS_PHASE_DIFFUSION:
+      enqueue_diffusion<S, A>(h, w, q);
+      settle(h, w, q);
       break;
-    }
-    case OS_PHASE_PROJECTION: {
-      if (h->block_k > 0 && blocked_supported<S, A>(h)) {
-        q.count += enqueue_blocked_projection<S, A>(h, st);
-        break;
-      }
-      const int half = (W + 1) / 2;
-      const dim3 gp((half + T - 1) / T, H);
-      for (int t = 0; t < c.n; t++) {
-        k_project_half<S, A, 0><<<gp, T, 0, st>>>(u, v, h->p, h->flags, c, h->d_params);
-        k_project_half<S, A, 1><<<gp, T, 0, st>>>(u, v, h->p, h->flags, c, h->d_params);
-        q.count += 2;
-      }
+    case OS_PHASE_PROJECTION:
+      enqueue_projection<S, A>(h, w, q, false);
+      settle(h, w, q);
       break;
-    }
     case OS_PHASE_PRESSURE_RANGE:
       k_prange_init<<<1, 32, 0, st>>>(h->d_pkeys);
       k_prange<<<152 * 4, 256, 0, st>>>(h->p, N, h->d_pkeys);
       q.count += 2;
       break;
     case OS_PHASE_EXTRAPOLATION:
-      k_extrapolate<S><<<1, 1024, 0, st>>>(u, v, c);
+      k_extrapolate<S><<<1, 1024, 0, st>>>(w.u(), w.v(), c);
       q.count++;
       break;
     case OS_PHASE_VEL_ADVECTION:
-      k_advect_velocity<S, A><<<g2, T, 0, st>>>(u, v, ub, vb, h->flags, c, h->d_params);
-      k_copy2<S><<<g1, 256, 0, st>>>(ub, vb, u, v, N);
-      q.count += 2;
+      k_advect_velocity<S, A><<<g2, 128, 0, st>>>(w.U[0], w.V[0], w.U[1], w.V[1], h->flags, c, h->d_params);
+      w.cu = w.cv = 1;
+      q.count++;
+      settle(h, w, q);
       break;
     case OS_PHASE_SMOKE_ADVECTION:
-      // Stand-alone phase: velocities are already in u, v.
-      k_advect_smoke<S, A, false><<<g2, T, 0, st>>>(u, v, s, sb, nullptr, nullptr, h->flags, c, h->d_params);
+      enqueue_smoke_advection<S, A>(h, w, q);
       k_copy1<S><<<g1, 256, 0, st>>>(sb, s, N);
-      q.count += 2;
-      break;
-    case OS_PHASE_DECAY: {
-      Consts cc = c;
-      k_finish_smoke<S, A><<<g1, 256, 0, st>>>(s, s, cc, h->d_params, N);
       q.count++;
       break;
-    }
+    case OS_PHASE_DECAY:
+      k_finish_smoke<S, A><<<g1, 256, 0, st>>>(s, s, c, h->d_params, N);
+      q.count++;
+      break;
     default:
       return set_err(OS_ERR_INVALID, "unknown phase %d", phase);
   }
@@ -190,37 +253,46 @@ int enqueue_phase(os_handle* h, int phase, Enq& q) {
   return OS_OK;
 }
 
-// Fluid::update (src/fluid.cu:770-795) as one fused launch sequence.
+// Fluid::update (src/fluid.cu:770-795) as one launch sequence. The order of
+// the phases is the reference's; copies between phases are avoided by
+// letting the live velocity alternate between the fields and their buffers.
 template <class S, class A>
 int enqueue_step(os_handle* h, Enq& q) {
   const os_config& cfg = h->cfg;
-  int rc;
-  if ((rc = enqueue_phase<S, A>(h, OS_PHASE_FORCES, q))) return rc;
-  if (cfg.enable_pressure && (rc = enqueue_phase<S, A>(h, OS_PHASE_ZERO_PRESSURE, q))) return rc;
-  if (cfg.viscosity != 0.0f && (rc = enqueue_phase<S, A>(h, OS_PHASE_DIFFUSION, q))) return rc;
-  if ((rc = enqueue_phase<S, A>(h, OS_PHASE_PROJECTION, q))) return rc;
-  if (cfg.enable_pressure && (rc = enqueue_phase<S, A>(h, OS_PHASE_PRESSURE_RANGE, q))) return rc;
-  if ((rc = enqueue_phase<S, A>(h, OS_PHASE_EXTRAPOLATION, q))) return rc;
-  S* u = static_cast<S*>(h->u);
-  S* v = static_cast<S*>(h->v);
+  Vel<S> w = vel_of<S>(h);
   S* s = static_cast<S*>(h->s);
-  S* ub = static_cast<S*>(h->ub);
-  S* vb = static_cast<S*>(h->vb);
   S* sb = static_cast<S*>(h->sb);
-  const int T = 128;
-  const dim3 g2((h->W + T - 1) / T, h->H);
+  const Consts& c = h->c;
+  const dim3 g2((h->W + 127) / 128, h->H);
   const int64_t N = (int64_t)h->N;
   const unsigned g1 = (unsigned)((N + 255) / 256);
-  k_advect_velocity<S, A><<<g2, T, 0, q.st>>>(u, v, ub, vb, h->flags, h->c, h->d_params);
+  k_forces<S, A><<<g2, 128, 0, q.st>>>(w.u(), w.v(), s, c, h->smoke_period, h->d_params);
+  q.count++;
+  // The blocked projection zeroes the pressure in its first pass.
+  if (cfg.enable_pressure && !(use_blocked<S, A>(h) && c.n > 0)) {
+    k_zero<<<g1, 256, 0, q.st>>>(h->p, N);
+    q.count++;
+  }
+  if (cfg.viscosity != 0.0f) enqueue_diffusion<S, A>(h, w, q);
+  enqueue_projection<S, A>(h, w, q, cfg.enable_pressure != 0);
+  if (cfg.enable_pressure) {
+    k_prange_init<<<1, 32, 0, q.st>>>(h->d_pkeys);
+    k_prange<<<152 * 4, 256, 0, q.st>>>(h->p, N, h->d_pkeys);
+    q.count += 2;
+  }
+  k_extrapolate<S><<<1, 1024, 0, q.st>>>(w.u(), w.v(), c);
+  q.count++;
+  k_advect_velocity<S, A><<<g2, 128, 0, q.st>>>(w.u(), w.v(), w.U[1 - w.cu], w.V[1 - w.cv],
+                                                 h->flags, c, h->d_params);
+  w.cu = 1 - w.cu;
+  w.cv = 1 - w.cv;
   q.count++;
   if (cfg.enable_smoke && cfg.tunnel_smoke != 0.0f) {
-    // smoke advection on the new velocities, copying them back as it goes
-    k_advect_smoke<S, A, true><<<g2, T, 0, q.st>>>(ub, vb, s, sb, u, v, h->flags, h->c, h->d_params);
-    k_finish_smoke<S, A><<<g1, 256, 0, q.st>>>(sb, s, h->c, h->d_params, N);
-    q.count += 2;
-  } else {
-    k_copy2<S><<<g1, 256, 0, q.st>>>(ub, vb, u, v, N);
+    enqueue_smoke_advection<S, A>(h, w, q);
+    k_finish_smoke<S, A><<<g1, 256, 0, q.st>>>(sb, s, c, h->d_params, N);
     q.count++;
+  } else {
+    settle(h, w, q);
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return set_err(OS_ERR_CUDA, "launch failed: %s", cudaGetErrorString(e));

@@ -131,6 +131,23 @@ def test_diffusion_matches_reference_to_race_order(gpu):
     assert same_bits(lib.download("vel_y"), ref.download("vel_y"))
 
 
+@pytest.mark.parametrize("block", [-1, 3])
+def test_diffusion_bit_exact_where_reference_is_race_free(gpu, block):
+    """On a 33x3 grid the reference's interior cells (i = 1..31, j = 1) are all
+    threads of one warp of one block (block_size_x = 64), which load before
+    they store: its in-place sweep is then exactly Jacobi, so the library must
+    match it bit for bit, sweep after sweep."""
+    cfg = default_config(33, 3)
+    cfg.viscosity = 7.0  # a = 0.35: every sweep changes every interior bit
+    cfg.projection_n = 9
+    cfg.projection_block = block
+    state = random_state(cfg, 14, np.zeros(33 * 3, np.int32))
+    lib, ref = load_lib(cfg, state), load_ref(cfg, state)
+    lib.run_phase(native.PHASE_DIFFUSION, None, 0.05)
+    ref.phase(native.PHASE_DIFFUSION, None, 0.05)
+    assert same_bits(lib.download("vel_x"), ref.download("vel_x"))
+
+
 @pytest.mark.parametrize("name,phase,src", PHASES + [("diffusion", native.PHASE_DIFFUSION, None)],
                          ids=[p[0] for p in PHASES] + ["diffusion"])
 def test_phase_vs_oracle(gpu, name, phase, src):
