@@ -111,9 +111,11 @@ typedef struct os_config {
   int32_t device;           /* CUDA device ordinal */
   int32_t projection_block; /* red/black sweeps fused per pass; 0 = autotune,
                                -1 = one launch per half-sweep (plain form) */
-  int32_t fast_idw;         /* 1: smoke inverse-distance weights in FP32; 0
-                               (default): in FP64 as the reference computes
-                               them (src/fluid.cu:690-693) */
+  int32_t idw_mode;         /* smoke inverse distances 1/(d + 1e-6), which the
+                               reference computes in FP64 (src/fluid.cu:
+                               690-693): 0 (default) FP32 float-pair
+                               arithmetic that rounds like the FP64
+                               expression; 1 literal FP64; 2 plain FP32 */
   int32_t reserved[4];
 } os_config;
 

@@ -19,6 +19,10 @@
 // despite the stride-2 colour pattern. Tiles and passes read one global copy
 // and write the other (fields <-> buffers), so no CTA reads a neighbour's
 // half-updated halo.
+//
+// Staging moves 4 consecutive cells per access (float4 / 32-bit flag words)
+// with several independent loads in flight per thread; cells off the grid
+// read as zero (they are never active and never feed an active cell).
 #pragma once
 
 #include <algorithm>
@@ -28,8 +32,10 @@ namespace osg {
 
 constexpr int kRegionW = 256;            // region width in cells
 constexpr int kHalfW = kRegionW / 2;     // cells per parity per row
-constexpr int kArrPad = 16;              // words between parity arrays (bank shift)
+constexpr int kQuads = kRegionW / 4;     // 4-cell groups per region row
+constexpr int kArrPad = 16;              // words between arrays (bank shift, alignment)
 constexpr int kBlockThreads = 1024;
+constexpr int kInFlight = 4;             // staging groups per thread per batch
 
 struct TileGeom {
   int halo;     // halo in cells on every side
@@ -47,6 +53,46 @@ __host__ __device__ inline size_t projection_smem(int RH, bool pressure) {
 
 __host__ __device__ inline size_t diffusion_smem(int RH) {
   return 2 * ((size_t)RH * kRegionW + kArrPad) * 4;
+}
+
+// Four consecutive cells (i..i+3) of logical row j, zero off the grid.
+// `vec` = rows start 16-byte aligned and i is a multiple of 4.
+__device__ __forceinline__ float4 load_quad(const float* __restrict__ f, int W, int H, int i,
+                                            int j, bool vec) {
+  float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (j < 0 || j >= H) return q;
+  const int64_t row = (int64_t)(H - 1 - j) * W;
+  if (vec && i >= 0 && i + 3 < W) return __ldg(reinterpret_cast<const float4*>(f + row + i));
+  if (i >= 0 && i < W) q.x = __ldg(f + row + i);
+  if (i + 1 >= 0 && i + 1 < W) q.y = __ldg(f + row + i + 1);
+  if (i + 2 >= 0 && i + 2 < W) q.z = __ldg(f + row + i + 2);
+  if (i + 3 >= 0 && i + 3 < W) q.w = __ldg(f + row + i + 3);
+  return q;
+}
+
+__device__ __forceinline__ uint32_t load_quad_u8(const uint8_t* __restrict__ f, int W, int H,
+                                                 int i, int j, bool vec) {
+  if (j < 0 || j >= H) return 0;
+  const int64_t row = (int64_t)(H - 1 - j) * W;
+  if (vec && i >= 0 && i + 3 < W) return __ldg(reinterpret_cast<const uint32_t*>(f + row + i));
+  uint32_t q = 0;
+#pragma unroll
+  for (int d = 0; d < 4; d++)
+    if (i + d >= 0 && i + d < W) q |= (uint32_t)__ldg(f + row + i + d) << (8 * d);
+  return q;
+}
+
+__device__ __forceinline__ void store_quad(float* __restrict__ f, int W, int H, int i, int j,
+                                           bool vec, float4 q) {
+  const int64_t row = (int64_t)(H - 1 - j) * W;
+  if (vec && i + 3 < W) {
+    *reinterpret_cast<float4*>(f + row + i) = q;
+    return;
+  }
+  if (i < W) f[row + i] = q.x;
+  if (i + 1 < W) f[row + i + 1] = q.y;
+  if (i + 2 < W) f[row + i + 2] = q.z;
+  if (i + 3 < W) f[row + i + 3] = q.w;
 }
 
 // ---------------------------------------------------------------------------
@@ -81,44 +127,109 @@ __device__ __forceinline__ ProjPlanes proj_planes(float* smem, int RH) {
 
 // One colour half-sweep over the region. Active cells of row y sit at
 // x = 2k + par with par = (y + COLOUR) & 1 (region origin has even global
-// coordinates, so local parity is global parity).
-template <int COLOUR, bool PRESSURE>
-__device__ __forceinline__ void proj_half_sweep(const ProjPlanes& P, int RH, const Consts& c,
-                                                float d_t) {
-  const int k = threadIdx.x & (kHalfW - 1);
-  const int rows_per_iter = blockDim.x / kHalfW;
-  for (int y = threadIdx.x / kHalfW; y < RH - 1; y += rows_per_iter) {
-    const int par = (y + COLOUR) & 1;
-    if (par && k == kHalfW - 1) continue;  // its right face lies outside the region
+// coordinates, so local parity is global parity). A thread keeps one k and
+// steps through rows 2*(blockDim/128) apart, so its parity, and with it every
+// plane offset, is fixed for the whole loop. Planes are addressed as word
+// offsets from the __shared__ base: ue 0, uo 1, ve 2, vo 3, pe 4, po 5 (x plane).
+// apply_projection_at (src/fluid.cu:229-262) for one cell given its four faces
+// and flag byte; faces it may not touch come back unchanged.
+template <bool PRESSURE>
+__device__ __forceinline__ void project_faces(uint32_t f, const Consts& c, float d_t, float& uc,
+                                              float& right_u, float& vc, float& top_v,
+                                              float& pc) {
+  if (!(f & F_ACTIVE)) return;
+  const float divergence = right_u - uc + top_v - vc;
+  const int sn = __popc(f & F_NBR_MASK);
+  // A rounded product: the reference keeps it (its later use sits behind a
+  // runtime branch) rather than fusing it into the four face updates.
+  const float velocity_diff = mul_rn(c.o, divergence / (float)sn);
+  if (PRESSURE) pc += velocity_diff * c.density * (float)c.h / d_t;  // src/fluid.cu:225-226
+  if (f & F_LEFT) uc = uc + velocity_diff;
+  if (f & F_RIGHT) right_u = right_u - velocity_diff;
+  if (f & F_BOTTOM) vc = vc + velocity_diff;
+  if (f & F_TOP) top_v = top_v - velocity_diff;
+}
+
+// A thread takes two neighbouring cells of the colour in one row (k, k+1:
+// x = 2k + par and 2k + 2 + par) and steps through rows 2*(blockDim/64)
+// apart, so its parity, and with it every plane offset, is fixed for the
+// whole loop. Faces move as 64-bit pairs; every face of a cell of this colour
+// belongs to that cell alone, so writing back unchanged faces is safe.
+// Planes are word offsets from the __shared__ base: ue 0, uo 1, ve 2, vo 3,
+// pe 4, po 5 (x plane).
+template <int PAR, bool PRESSURE>
+__device__ __forceinline__ void proj_rows(float* __restrict__ S, const uint8_t* __restrict__ F,
+                                          int plane, int fo_off, const Consts& c, float d_t,
+                                          int k, int y_begin, int y_end, int rows_per_iter) {
+  // With PAR = 1 the cell at k = 127 has its right face outside the region.
+  const bool second = !(PAR && k == kHalfW - 2);
+  const int oL = PAR ? plane : 0;      // plane of the left face u(x)
+  const int oR = plane - oL;           // plane of the right face u(x+1)
+  const int oV = 2 * plane + oL;       // plane of v(x, .)
+  const int oP = 4 * plane + oL;       // plane of p(x, .)
+  const int oF = PAR ? fo_off : 0;
+  for (int y = y_begin; y < y_end; y += rows_per_iter) {
     const int s = y * kHalfW + k;
-    const uint8_t f = (par ? P.fo : P.fe)[s];
-    if (!(f & F_ACTIVE)) continue;
-    float* uL = par ? P.uo : P.ue;   // left face u(x)     at s
-    float* uR = par ? P.ue : P.uo;   // right face u(x+1)  at sr
-    float* vv = par ? P.vo : P.ve;   // v(x, y) at s, v(x, y+1) at s + kHalfW
-    const int sr = s + par;
-    const float uc = uL[s];
-    const float vc = vv[s];
-    const float top_v = vv[s + kHalfW];
-    const float right_u = uR[sr];
-    const float divergence = right_u - uc + top_v - vc;
-    const int sn = __popc(f & F_NBR_MASK);
-    // A rounded product: the reference keeps it (its later use sits behind a
-    // runtime branch) rather than fusing it into the four face updates.
-    const float velocity_diff = mul_rn(c.o, divergence / (float)sn);
-    if (PRESSURE) {
-      float* pp = par ? P.po : P.pe;
-      pp[s] += velocity_diff * c.density * (float)c.h / d_t;  // src/fluid.cu:225-226
+    const uint32_t f2 = *reinterpret_cast<const uint16_t*>(F + oF + s);
+    if (!(f2 & (F_ACTIVE | (F_ACTIVE << 8)))) continue;
+    float2 uL = *reinterpret_cast<const float2*>(S + oL + s);
+    float2 vB = *reinterpret_cast<const float2*>(S + oV + s);
+    float2 vT = *reinterpret_cast<const float2*>(S + oV + s + kHalfW);
+    float2 uR;
+    if (PAR) {
+      uR.x = S[oR + s + 1];
+      uR.y = second ? S[oR + s + 2] : 0.0f;
+    } else {
+      uR = *reinterpret_cast<const float2*>(S + oR + s);
     }
-    if (f & F_LEFT) uL[s] = uc + velocity_diff;
-    if (f & F_RIGHT) uR[sr] = right_u - velocity_diff;
-    if (f & F_BOTTOM) vv[s] = vc + velocity_diff;
-    if (f & F_TOP) vv[s + kHalfW] = top_v - velocity_diff;
+    float2 pp = make_float2(0.0f, 0.0f);
+    if (PRESSURE) pp = *reinterpret_cast<const float2*>(S + oP + s);
+    project_faces<PRESSURE>(f2 & 0xffu, c, d_t, uL.x, uR.x, vB.x, vT.x, pp.x);
+    if (second) project_faces<PRESSURE>(f2 >> 8, c, d_t, uL.y, uR.y, vB.y, vT.y, pp.y);
+    *reinterpret_cast<float2*>(S + oL + s) = uL;
+    *reinterpret_cast<float2*>(S + oV + s) = vB;
+    *reinterpret_cast<float2*>(S + oV + s + kHalfW) = vT;
+    if (PAR) {
+      S[oR + s + 1] = uR.x;
+      if (second) S[oR + s + 2] = uR.y;
+    } else {
+      *reinterpret_cast<float2*>(S + oR + s) = uR;
+    }
+    if (PRESSURE) *reinterpret_cast<float2*>(S + oP + s) = pp;
   }
+}
+
+// `reach`: the half-sweeps still to come in this pass. A face stored in an
+// owned cell is last written by that cell or by its left / lower neighbour,
+// and every earlier half-sweep widens that set by one cell per side, so only
+// cells in [halo - 1 - reach, size - halo + reach) on each axis are computed;
+// the rest of the region is stale and never reaches an owned face.
+template <int COLOUR, bool PRESSURE>
+__device__ __forceinline__ void proj_half_sweep(float* __restrict__ S,
+                                                const uint8_t* __restrict__ F, int plane,
+                                                int fo_off, int RH, int halo, int reach,
+                                                const Consts& c, float d_t) {
+  constexpr int kPairs = kHalfW / 2;
+  const int k = 2 * (threadIdx.x % kPairs);
+  const int rows_per_iter = blockDim.x / kPairs;  // even
+  const int y0 = threadIdx.x / kPairs;
+  const int par = (y0 + COLOUR) & 1;
+  const int lo = max(0, halo - 1 - reach);        // first needed cell, both axes
+  const int x = 2 * k + par;                      // the pair covers x .. x + 2
+  if (x + 2 < lo || x >= kRegionW - halo + reach) return;
+  const int y_end = min(RH - 1, RH - halo + reach);
+  const int skip = lo > y0 ? (lo - y0 + rows_per_iter - 1) / rows_per_iter : 0;
+  const int y_begin = y0 + skip * rows_per_iter;
+  if (par)
+    proj_rows<1, PRESSURE>(S, F, plane, fo_off, c, d_t, k, y_begin, y_end, rows_per_iter);
+  else
+    proj_rows<0, PRESSURE>(S, F, plane, fo_off, c, d_t, k, y_begin, y_end, rows_per_iter);
 }
 
 // With PRESSURE the first pass of a step zeroes p (zero_pressure,
 // src/fluid.cu:203-219) as it loads; later passes continue the accumulation.
+// p is staged for owned cells only (halo pressure is never needed), so no CTA
+// reads pressure that another CTA writes in the same pass.
 template <bool PRESSURE>
 __global__ void __launch_bounds__(kBlockThreads, 1)
 k_project_blocked(const float* __restrict__ u_in, const float* __restrict__ v_in,
@@ -131,46 +242,86 @@ k_project_blocked(const float* __restrict__ u_in, const float* __restrict__ v_in
   const int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
   const int gx0 = tx * TX - halo, gy0 = ty * TY - halo;
   const int W = c.W, H = c.H;
-  for (int e = threadIdx.x; e < RH * kRegionW; e += blockDim.x) {
-    const int y = e / kRegionW, x = e % kRegionW;
-    const int i = gx0 + x, j = gy0 + y;
-    float uu = 0.0f, vv = 0.0f, pp = 0.0f;
-    uint8_t ff = 0;
-    if (i >= 0 && i < W && j >= 0 && j < H) {
-      const int64_t gk = cell_index(W, H, i, j);
-      uu = u_in[gk];
-      vv = v_in[gk];
-      ff = fl[gk];
-      if (PRESSURE && !zero_pressure && x >= halo && x < halo + TX && y >= halo && y < halo + TY)
-        pp = p[gk];
+  const bool vec = ((W & 3) == 0) && ((gx0 & 3) == 0);
+  const int items = RH * kQuads;
+  for (int base = threadIdx.x; base < items; base += blockDim.x * kInFlight) {
+    float4 uq[kInFlight], vq[kInFlight];
+    uint32_t fq[kInFlight];
+#pragma unroll
+    for (int r = 0; r < kInFlight; r++) {
+      const int it = base + r * blockDim.x;
+      const int y = it / kQuads, x = 4 * (it % kQuads);
+      const bool ok = it < items;
+      uq[r] = ok ? load_quad(u_in, W, H, gx0 + x, gy0 + y, vec) : make_float4(0.f, 0.f, 0.f, 0.f);
+      vq[r] = ok ? load_quad(v_in, W, H, gx0 + x, gy0 + y, vec) : make_float4(0.f, 0.f, 0.f, 0.f);
+      fq[r] = ok ? load_quad_u8(fl, W, H, gx0 + x, gy0 + y, vec) : 0u;
     }
-    const int s = y * kHalfW + (x >> 1);
-    if (x & 1) {
-      P.uo[s] = uu; P.vo[s] = vv; P.fo[s] = ff;
-      if (PRESSURE) P.po[s] = pp;
-    } else {
-      P.ue[s] = uu; P.ve[s] = vv; P.fe[s] = ff;
-      if (PRESSURE) P.pe[s] = pp;
+#pragma unroll
+    for (int r = 0; r < kInFlight; r++) {
+      const int it = base + r * blockDim.x;
+      if (it >= items) break;
+      const int y = it / kQuads, q = it % kQuads;
+      const int s = y * kHalfW + 2 * q;  // cells 4q, 4q+2 -> even plane; 4q+1, 4q+3 -> odd
+      *reinterpret_cast<float2*>(P.ue + s) = make_float2(uq[r].x, uq[r].z);
+      *reinterpret_cast<float2*>(P.uo + s) = make_float2(uq[r].y, uq[r].w);
+      *reinterpret_cast<float2*>(P.ve + s) = make_float2(vq[r].x, vq[r].z);
+      *reinterpret_cast<float2*>(P.vo + s) = make_float2(vq[r].y, vq[r].w);
+      const uint32_t f = fq[r];
+      *reinterpret_cast<uint16_t*>(P.fe + s) = (uint16_t)((f & 0xffu) | ((f >> 8) & 0xff00u));
+      *reinterpret_cast<uint16_t*>(P.fo + s) = (uint16_t)(((f >> 8) & 0xffu) | ((f >> 16) & 0xff00u));
+    }
+  }
+  if (PRESSURE) {
+    for (int e = threadIdx.x; e < RH * kRegionW; e += blockDim.x) {
+      const int y = e / kRegionW, x = e % kRegionW;
+      const int i = gx0 + x, j = gy0 + y;
+      float pp = 0.0f;
+      if (!zero_pressure && x >= halo && x < halo + TX && y >= halo && y < halo + TY && i < W &&
+          j < H)
+        pp = p[cell_index(W, H, i, j)];
+      ((x & 1) ? P.po : P.pe)[y * kHalfW + (x >> 1)] = pp;
     }
   }
   __syncthreads();
   const float d_t = prm->dt;
+  const int plane = RH * kHalfW + kArrPad;
+  const int fo_off = RH * kHalfW + 64;
   for (int t = 0; t < sweeps; t++) {
-    proj_half_sweep<0, PRESSURE>(P, RH, c, d_t);
+    const int reach = 2 * (sweeps - t) - 1;  // half-sweeps after the even one
+    proj_half_sweep<0, PRESSURE>(smem, P.fe, plane, fo_off, RH, halo, reach, c, d_t);
     __syncthreads();
-    proj_half_sweep<1, PRESSURE>(P, RH, c, d_t);
+    proj_half_sweep<1, PRESSURE>(smem, P.fe, plane, fo_off, RH, halo, reach - 1, c, d_t);
     __syncthreads();
   }
-  for (int e = threadIdx.x; e < TY * kRegionW; e += blockDim.x) {
-    const int y = halo + e / kRegionW, x = e % kRegionW;
-    if (x < halo || x >= halo + TX) continue;
+  // Owned cells back out; halo and TX are multiples of 4 when `vec` holds.
+  for (int it = threadIdx.x; it < TY * kQuads; it += blockDim.x) {
+    const int y = halo + it / kQuads, x = 4 * (it % kQuads);
     const int i = gx0 + x, j = gy0 + y;
-    if (i >= W || j >= H) continue;
-    const int64_t gk = cell_index(W, H, i, j);
+    if (j >= H || i >= W) continue;
     const int s = y * kHalfW + (x >> 1);
-    u_out[gk] = (x & 1) ? P.uo[s] : P.ue[s];
-    v_out[gk] = (x & 1) ? P.vo[s] : P.ve[s];
-    if (PRESSURE) p[gk] = (x & 1) ? P.po[s] : P.pe[s];
+    if (vec && x >= halo && x + 3 < halo + TX) {
+      const float2 ue = *reinterpret_cast<const float2*>(P.ue + s);
+      const float2 uo = *reinterpret_cast<const float2*>(P.uo + s);
+      const float2 ve = *reinterpret_cast<const float2*>(P.ve + s);
+      const float2 vo = *reinterpret_cast<const float2*>(P.vo + s);
+      store_quad(u_out, W, H, i, j, true, make_float4(ue.x, uo.x, ue.y, uo.y));
+      store_quad(v_out, W, H, i, j, true, make_float4(ve.x, vo.x, ve.y, vo.y));
+      if (PRESSURE) {
+        const float2 pe = *reinterpret_cast<const float2*>(P.pe + s);
+        const float2 po = *reinterpret_cast<const float2*>(P.po + s);
+        store_quad(p, W, H, i, j, true, make_float4(pe.x, po.x, pe.y, po.y));
+      }
+      continue;
+    }
+    for (int d = 0; d < 4; d++) {
+      const int xd = x + d;
+      if (xd < halo || xd >= halo + TX || i + d >= W) continue;
+      const int64_t gk = cell_index(W, H, i + d, j);
+      const int sd = y * kHalfW + (xd >> 1);
+      u_out[gk] = (xd & 1) ? P.uo[sd] : P.ue[sd];
+      v_out[gk] = (xd & 1) ? P.vo[sd] : P.ve[sd];
+      if (PRESSURE) p[gk] = (xd & 1) ? P.po[sd] : P.pe[sd];
+    }
   }
 }
 
@@ -188,26 +339,55 @@ k_diffuse_blocked(const float* __restrict__ u_in, float* __restrict__ u_out, Con
   const int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
   const int gx0 = tx * TX - halo, gy0 = ty * TY - halo;
   const int W = c.W, H = c.H;
-  for (int e = threadIdx.x; e < RH * kRegionW; e += blockDim.x) {
-    const int y = e / kRegionW, x = e % kRegionW;
-    const int i = gx0 + x, j = gy0 + y;
-    A[e] = (i >= 0 && i < W && j >= 0 && j < H) ? u_in[cell_index(W, H, i, j)] : 0.0f;
+  const bool vec = ((W & 3) == 0) && ((gx0 & 3) == 0);
+  const int items = RH * kQuads;
+  for (int base = threadIdx.x; base < items; base += blockDim.x * kInFlight) {
+    float4 uq[kInFlight];
+#pragma unroll
+    for (int r = 0; r < kInFlight; r++) {
+      const int it = base + r * blockDim.x;
+      const int y = it / kQuads, x = 4 * (it % kQuads);
+      uq[r] = it < items ? load_quad(u_in, W, H, gx0 + x, gy0 + y, vec)
+                         : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+#pragma unroll
+    for (int r = 0; r < kInFlight; r++) {
+      const int it = base + r * blockDim.x;
+      if (it >= items) break;
+      // Both buffers: cells that no sweep updates keep their value in each.
+      *reinterpret_cast<float4*>(A + 4 * it) = uq[r];
+      *reinterpret_cast<float4*>(B + 4 * it) = uq[r];
+    }
   }
   __syncthreads();
   const float d_t = prm->dt;
   const float a = c.viscosity * d_t / (float)(c.h * c.h);
+  // Updated cells: domain interior and not on the region's outer ring. A
+  // thread owns one column and a contiguous run of rows, carrying the column
+  // neighbours (j-1, j, j+1) in registers.
+  const int x = threadIdx.x % kRegionW;
+  const int groups = blockDim.x / kRegionW;
+  const int i = gx0 + x;
+  const int y_lo = max(1, 1 - gy0), y_hi = min(RH - 2, H - 2 - gy0);
+  const int chunk = (y_hi - y_lo + groups) / groups;
+  const int r0 = y_lo + (threadIdx.x / kRegionW) * chunk;
+  const int r1 = min(y_hi + 1, r0 + chunk);
+  const bool column = x > 0 && x < kRegionW - 1 && i > 0 && i < W - 1 && r0 < r1;
   for (int t = 0; t < sweeps; t++) {
-    for (int e = threadIdx.x; e < RH * kRegionW; e += blockDim.x) {
-      const int y = e / kRegionW, x = e % kRegionW;
-      const int i = gx0 + x, j = gy0 + y;
-      const bool interior = i > 0 && j > 0 && i < W - 1 && j < H - 1 && x > 0 &&
-                            x < kRegionW - 1 && y > 0 && y < RH - 1;
-      if (interior) {
+    // Only cells within `reach` (sweeps still to come) of the owned tile can
+    // still influence it.
+    const int reach = sweeps - 1 - t;
+    const int ya = max(r0, halo - reach), yb = min(r1, RH - halo + reach);
+    if (column && x >= halo - reach && x < kRegionW - halo + reach && ya < yb) {
+      float down = A[(ya - 1) * kRegionW + x];
+      float centre = A[ya * kRegionW + x];
+      for (int y = ya; y < yb; y++) {
+        const int e = y * kRegionW + x;
+        const float up = A[e + kRegionW];
         // src/fluid.cu:178-182: neighbours (i-1, j), (i+1, j), (i, j-1), (i, j+1)
-        B[e] = (A[e] + a * (A[e - 1] + A[e + 1] + A[e - kRegionW] + A[e + kRegionW])) /
-               (1 + 4 * a);
-      } else {
-        B[e] = A[e];
+        B[e] = (centre + a * (A[e - 1] + A[e + 1] + down + up)) / (1 + 4 * a);
+        down = centre;
+        centre = up;
       }
     }
     __syncthreads();
@@ -215,12 +395,19 @@ k_diffuse_blocked(const float* __restrict__ u_in, float* __restrict__ u_out, Con
     A = B;
     B = T;
   }
-  for (int e = threadIdx.x; e < TY * kRegionW; e += blockDim.x) {
-    const int y = halo + e / kRegionW, x = e % kRegionW;
-    if (x < halo || x >= halo + TX) continue;
+  for (int it = threadIdx.x; it < TY * kQuads; it += blockDim.x) {
+    const int y = halo + it / kQuads, x = 4 * (it % kQuads);
     const int i = gx0 + x, j = gy0 + y;
-    if (i >= W || j >= H) continue;
-    u_out[cell_index(W, H, i, j)] = A[y * kRegionW + x];
+    if (j >= H || i >= W) continue;
+    const float* src = A + y * kRegionW + x;
+    if (vec && x >= halo && x + 3 < halo + TX) {
+      store_quad(u_out, W, H, i, j, true, *reinterpret_cast<const float4*>(src));
+      continue;
+    }
+    for (int d = 0; d < 4; d++) {
+      if (x + d < halo || x + d >= halo + TX || i + d >= W) continue;
+      u_out[cell_index(W, H, i + d, j)] = src[d];
+    }
   }
 }
 
@@ -271,8 +458,8 @@ inline int sm_count(int device) {
 }
 
 // Projection: ceil(n / K) passes of up to K sweeps; each pass reads one copy of
-// (u, v) and writes the other. `cur` tracks which copy holds the live field
-// (0: u/v, 1: ub/vb) and is updated for the caller.
+// (u, v) and writes the other. `cur_u`/`cur_v` track which copy holds the
+// live field (0: u/v, 1: ub/vb) and are updated for the caller.
 // `zero_first`: the first pass also performs zero_pressure (inside a step).
 inline int enqueue_blocked_projection_f32(os_handle* h, cudaStream_t st, int* cur_u, int* cur_v,
                                           bool zero_first) {

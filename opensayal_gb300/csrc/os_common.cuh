@@ -36,7 +36,7 @@ struct Consts {
   float speed, tunnel_smoke, decay_rate;
   int smoke_length, smoke_count, smoke_height, pipe_height;
   int enable_decay, enable_pressure;
-  int fast_idw;        // 1: inverse-distance weights in FP32 instead of FP64
+  int idw_mode;        // smoke inverse distances: 0 FP32 pair, 1 FP64, 2 FP32
 };
 
 // Per-step inputs, kept in device memory so that one captured graph serves

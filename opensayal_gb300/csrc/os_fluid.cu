@@ -373,6 +373,7 @@ int validate(const os_config* c) {
   if (c->block_size_x < 1 || c->block_size_y < 1)
     return set_err(OS_ERR_INVALID, "thread.cuda.block_size_* must be >= 1");
   if (storage_bytes(c->storage) == 0) return set_err(OS_ERR_INVALID, "unknown storage %d", c->storage);
+  if (c->idw_mode < 0 || c->idw_mode > 2) return set_err(OS_ERR_INVALID, "idw_mode must be 0, 1 or 2");
   if (c->smoke_count != 1) {
     if (c->smoke_count - 1 == 0) return set_err(OS_ERR_INVALID, "smoke_count");
     const int spacing = (c->pipe_height - c->smoke_count * c->smoke_height) / (c->smoke_count - 1);
@@ -502,7 +503,7 @@ int os_config_defaults(int32_t width, int32_t height, os_config* out) {
   out->storage = OS_STORAGE_F32;
   out->device = 0;
   out->projection_block = 0;
-  out->fast_idw = 0;
+  out->idw_mode = 0;
   return OS_OK;
 }
 
@@ -538,7 +539,7 @@ int os_create(const os_config* cfg, os_handle** out) {
   c.pipe_height = cfg->pipe_height;
   c.enable_decay = cfg->smoke_enable_decay != 0;
   c.enable_pressure = cfg->enable_pressure != 0;
-  c.fast_idw = cfg->fast_idw != 0;
+  c.idw_mode = cfg->idw_mode;
   if (cfg->smoke_count != 1) {
     const int spacing = (cfg->pipe_height - cfg->smoke_count * cfg->smoke_height) /
                         (cfg->smoke_count - 1);

@@ -64,7 +64,7 @@ class OsConfig(C.Structure):
         ("storage", C.c_int32),
         ("device", C.c_int32),
         ("projection_block", C.c_int32),
-        ("fast_idw", C.c_int32),
+        ("idw_mode", C.c_int32),
         ("reserved", C.c_int32 * 4),
     ]
 

@@ -45,7 +45,7 @@ def _c_layout() -> dict:
 int main(void) {
   printf("os_config %zu\nos_source %zu\nos_fields_view %zu\n",
          sizeof(os_config), sizeof(os_source), sizeof(os_fields_view));
-  F(os_config, viscosity) F(os_config, storage) F(os_config, fast_idw)
+  F(os_config, viscosity) F(os_config, storage) F(os_config, idw_mode)
   F(os_config, obstacle_radius) F(os_source, position_y) F(os_fields_view, total_s)
   return 0;
 }
@@ -67,7 +67,7 @@ def test_ctypes_mirror_matches_c_layout():
     assert lay["os_source"] == C.sizeof(native.OsSource)
     assert lay["os_fields_view"] == C.sizeof(native.OsFieldsView)
     for key, cls in [("os_config.viscosity", native.OsConfig), ("os_config.storage", native.OsConfig),
-                     ("os_config.fast_idw", native.OsConfig),
+                     ("os_config.idw_mode", native.OsConfig),
                      ("os_config.obstacle_radius", native.OsConfig),
                      ("os_source.position_y", native.OsSource),
                      ("os_fields_view.total_s", native.OsFieldsView)]:
@@ -91,7 +91,7 @@ def test_defaults_follow_config_parser(lib_built):
     assert c.obstacle_radius == np.float32(1080 / 30.0)
     assert c.density == 1.0 and c.drag_coeff == 0.0
     assert c.viscosity == np.float32(0.001)
-    assert c.storage == 0 and c.fast_idw == 0
+    assert c.storage == 0 and c.idw_mode == 0
 
 
 def test_load_config_dotted_and_nested_keys(lib_built):
