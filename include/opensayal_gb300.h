@@ -229,6 +229,29 @@ int os_kernel_launches(os_handle* h, int64_t* out);
 int os_profile_phase(os_handle* h, int32_t phase, const os_source* src, float dt,
                      int32_t reps, void* stream, float* ms_out, int32_t* kernels_out);
 
+/*
+ * The diffusion phase (n Jacobi sweeps of u, as OS_PHASE_DIFFUSION runs it)
+ * on a caller-owned device field, without allocating anything. No counterpart
+ * in the reference: it is for callers that may not allocate device memory
+ * where they run a step (memory owned by another allocator, a frame loop that
+ * cannot afford an allocation's synchronisation, a fixed device footprint).
+ *
+ * `u` is width*height floats in the reference layout on the calling thread's
+ * current device; it is read and overwritten in place. Only width, height,
+ * cell_size, projection_n and viscosity of `cfg` are used. The work is
+ * enqueued on `stream` (a cudaStream_t; NULL is the legacy default stream)
+ * and the call returns without waiting.
+ *
+ * The ping-pong buffer is one fixed device array inside the library of
+ * 1,048,576 floats (4 MiB, held on every GPU that loads the library until it
+ * is unloaded); larger grids are rejected with OS_ERR_INVALID. The first call
+ * on a device looks up that array's device address (with the device current)
+ * and should come before any stream capture. All calls on a device share the
+ * array and it keeps the last call's contents; calls that overlap on the GPU
+ * (other streams, or other threads) race on it and must be serialised.
+ */
+int os_diffuse_noalloc(const os_config* cfg, float* u, float dt, void* stream);
+
 #ifdef __cplusplus
 }  /* extern "C" */
 #endif

@@ -16,6 +16,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <vector>
 
@@ -764,3 +765,109 @@ int os_profile_phase(os_handle* h, int32_t phase, const os_source* src, float dt
 }
 
 }  // extern "C"
+
+// ===========================================================================
+// Allocation-free diffusion
+//
+// Some callers cannot allocate device memory at the moment they want to run
+// a step: code whose memory is owned by another allocator (a framework pool
+// or a renderer that forbids stray cudaMalloc/cudaFree calls), code on a
+// real-time frame path where an allocation's implicit synchronisation would
+// stall the frame, and code that must keep a fixed device footprint. For them
+// the diffusion phase runs on a caller-owned field with the Jacobi ping-pong
+// buffer taken from a fixed array in the library's own device memory instead
+// of from a handle's buffers.
+// ===========================================================================
+
+namespace {
+
+// Largest grid (width * height) os_diffuse_noalloc accepts: 1 Mi cells, e.g.
+// 1024 x 1024. The array costs 4 MiB on every GPU that loads the library, for
+// as long as the library stays loaded.
+constexpr size_t kNoAllocMaxCells = size_t(1) << 20;
+
+static __device__ __align__(256) float g_noalloc_scratch[kNoAllocMaxCells];
+
+// Device address of g_noalloc_scratch on each device, looked up once per
+// device with that device current. In host code the symbol itself only names
+// a host-side shadow and must never be passed to a kernel.
+constexpr int kNoAllocMaxDevices = 64;
+float* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+std::mutex g_noalloc_mu;
+
+int noalloc_scratch(int device, float** out) {
+  if (device < 0 || device >= kNoAllocMaxDevices)
+    return set_err(OS_ERR_INVALID, "device %d out of range", device);
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_ptr[device]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+      return set_err(OS_ERR_CUDA, "cudaGetSymbolAddress(noalloc scratch): %s",
+                     cudaGetErrorString(e));
+    g_noalloc_ptr[device] = static_cast<float*>(p);
+  }
+  *out = g_noalloc_ptr[device];
+  return OS_OK;
+}
+
+// k_diffuse's sweep with dt passed by value (no device parameter block).
+__global__ void k_diffuse_noalloc(const float* __restrict__ uin, float* __restrict__ uout,
+                                  Consts c, float d_t) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y;
+  if (i >= c.W) return;
+  const int W = c.W;
+  const int64_t k = cell_index(W, c.H, i, j);
+  if (i >= W - 1 || j >= c.H - 1 || i <= 0 || j <= 0) {
+    uout[k] = uin[k];
+    return;
+  }
+  float a = c.viscosity * d_t / (float)(c.h * c.h);
+  float val = (uin[k] + a * (uin[k - 1] + uin[k + 1] + uin[k + W] + uin[k - W])) / (1 + 4 * a);
+  uout[k] = val;
+}
+
+}  // namespace
+
+extern "C" int os_diffuse_noalloc(const os_config* cfg, float* u, float dt, void* stream) {
+  if (!cfg || !u) return set_err(OS_ERR_INVALID, "null argument");
+  if (cfg->width < 3 || cfg->height < 3)
+    return set_err(OS_ERR_INVALID, "grid must be at least 3x3 (got %dx%d)", cfg->width,
+                   cfg->height);
+  if ((int)cfg->cell_size < 1)
+    return set_err(OS_ERR_INVALID, "sim.cell_size must be >= 1 (Fluid truncates it to int)");
+  if (cfg->projection_n < 0) return set_err(OS_ERR_INVALID, "sim.projection.n must be >= 0");
+  const size_t N = (size_t)cfg->width * (size_t)cfg->height;
+  if (N > kNoAllocMaxCells)
+    return set_err(OS_ERR_INVALID,
+                   "os_diffuse_noalloc: %dx%d = %zu cells exceeds its fixed scratch of %zu cells",
+                   cfg->width, cfg->height, N, kNoAllocMaxCells);
+  int device = 0;
+  CUDA_OR_RETURN(cudaGetDevice(&device));
+  float* scratch = nullptr;
+  int rc = noalloc_scratch(device, &scratch);
+  if (rc) return rc;
+  if (cfg->viscosity == 0.0f || cfg->projection_n == 0) return OS_OK;
+  Consts c{};
+  c.W = cfg->width;
+  c.H = cfg->height;
+  c.h = (int)cfg->cell_size;
+  c.n = cfg->projection_n;
+  c.viscosity = cfg->viscosity;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const dim3 g2((c.W + 127) / 128, c.H);
+  // Every sweep writes every cell of its output, so the scratch needs no
+  // clearing: nothing is read from it before this call has written it.
+  for (int t = 0; t < c.n; t++) {
+    const float* in = (t & 1) ? scratch : u;
+    float* out = (t & 1) ? u : scratch;
+    k_diffuse_noalloc<<<g2, 128, 0, st>>>(in, out, c, dt);
+  }
+  if (c.n & 1) {
+    const int64_t n = (int64_t)N;
+    k_copy1<float><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(scratch, u, n);
+  }
+  CUDA_OR_RETURN(cudaGetLastError());
+  return OS_OK;
+}
