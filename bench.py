@@ -136,7 +136,7 @@ def dist_max(world, x: float) -> float:
     return float(t.item())
 
 
-def cpu_baseline(cfg, budget_s: float = 12.0, max_steps: int = 60) -> dict:
+def cpu_baseline(cfg, budget_s: float = 15.0, max_steps: int = 400) -> dict:
     """The oracle port on the host cores (rank 0, N=1 only)."""
     import oracle
     from opensayal_gb300 import scenarios
@@ -238,11 +238,13 @@ def run_gb300(args, world, rank, local) -> dict | None:
     proj_bytes = 17 * cfg.projection_n * cells
     diff_ms, diff_kernels = f.profile_phase(native.PHASE_DIFFUSION, None, dt, 3, sptr)
     achieved = proj_bytes / proj_s / 1e9
+    # DRAM bytes per projection launch from the ncu capture summarised in
+    # profiles/ (same workload and blocking depth), or null.
     traffic = None
     tfile = ROOT / "profiles" / "roofline_traffic.json"
     if tfile.exists():
-        t = json.loads(tfile.read_text()).get(f"{args.workload}:block{cfg.projection_block}")
-        traffic = t
+        key = f"{args.workload}:block{f.fields().projection_block}"
+        traffic = json.loads(tfile.read_text()).get(key)
     step_bytes = bytes_per_cell_step(cfg.projection_n, cfg.viscosity != 0.0)
     ms_per_step = total_s * 1e3 / args.steps
     result = {
@@ -253,7 +255,8 @@ def run_gb300(args, world, rank, local) -> dict | None:
         "config": config_record(cfg, args.workload, {
             "parallelism": "replicas" if world > 1 else "single", "global_batch": world,
             "kernels_per_step": launches // max(1, args.steps),
-            "projection_block": cfg.projection_block}),
+            "projection_block": f.fields().projection_block,
+            "projection_block_source": "autotuned" if cfg.projection_block == 0 else "fixed"}),
         "e2e": e2e,
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"],

@@ -109,8 +109,11 @@ typedef struct os_config {
   /* Extensions with no reference key. Zero means "reference behaviour". */
   int32_t storage;          /* os_storage of u, v, smoke; 0 = FP32 */
   int32_t device;           /* CUDA device ordinal */
-  int32_t projection_block; /* red/black sweeps fused per pass; 0 = autotune,
-                               -1 = one launch per half-sweep (plain form) */
+  int32_t projection_block; /* red/black (and Jacobi) sweeps fused per pass;
+                               0 = autotune: os_create times candidate depths
+                               on a scratch grid of the same configuration
+                               once per process and configuration shape;
+                               -1 = one launch per sweep (plain form) */
   int32_t idw_mode;         /* smoke inverse distances 1/(d + 1e-6), which the
                                reference computes in FP64 (src/fluid.cu:
                                690-693): 0 (default) FP32 float-pair
@@ -133,7 +136,7 @@ typedef struct os_fields_view {
   int32_t width;
   int32_t height;
   int32_t storage;    /* os_storage of vel_x, vel_y, smoke */
-  int32_t reserved;
+  int32_t projection_block; /* sweeps per blocked pass in use (-1: plain) */
   void* vel_x;        /* Fluid::d_vel_x */
   void* vel_y;        /* Fluid::d_vel_y */
   void* smoke;        /* Fluid::d_smoke */

@@ -439,10 +439,12 @@ inline TileGeom make_geom(int W, int H, int halo, bool projection, bool pressure
   return g;
 }
 
+// Sweeps per blocked pass as configured: -1 plain, K > 0 fixed, 0 = to be
+// chosen by the autotuner once the handle exists.
 inline int choose_block_k(const os_handle* h) {
   if (h->cfg.projection_block < 0) return -1;
   if (h->cfg.projection_block > 0) return std::min(h->cfg.projection_block, 32);
-  return 4;
+  return 0;
 }
 
 template <class S, class A>

@@ -15,9 +15,12 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <new>
+#include <tuple>
 #include <vector>
 
 #include "../../include/opensayal_gb300.h"
@@ -385,6 +388,8 @@ int validate(const os_config* c) {
   return OS_OK;
 }
 
+int autotune_block_k(const os_config& base);
+
 void free_handle(os_handle* h) {
   if (!h) return;
   if (h->graph) cudaGraphExecDestroy(h->graph);
@@ -592,6 +597,8 @@ int os_create(const os_config* cfg, os_handle** out) {
   if ((e = cudaGetLastError()) != cudaSuccess ||
       (e = cudaStreamSynchronize(h->stream)) != cudaSuccess)
     return fail(set_err(OS_ERR_CUDA, "init: %s", cudaGetErrorString(e)));
+  if (h->block_k == 0)
+    h->block_k = h->storage == OS_STORAGE_F32 ? autotune_block_k(*cfg) : -1;
   *out = h;
   return OS_OK;
 }
@@ -643,6 +650,7 @@ int os_fields(os_handle* h, os_fields_view* out) {
   out->width = h->W;
   out->height = h->H;
   out->storage = h->storage;
+  out->projection_block = h->block_k;
   out->vel_x = h->u;
   out->vel_y = h->v;
   out->smoke = h->s;
@@ -765,6 +773,84 @@ int os_profile_phase(os_handle* h, int32_t phase, const os_source* src, float dt
 }
 
 }  // extern "C"
+
+// ===========================================================================
+// Autotuner for the blocking depth
+//
+// The best number of sweeps per blocked pass depends on the grid: a deeper
+// pass stages the field fewer times but recomputes a wider halo and, at some
+// depth, no longer fits one tile per SM. os_create with projection_block == 0
+// times each candidate depth on a scratch grid of the same configuration
+// (2 warm-up steps, then 3 timed with CUDA events) and keeps the fastest. The
+// answer is cached per process for the configuration's shape, so later
+// handles of the same shape pay nothing. OPENSAYAL_GB300_AUTOTUNE=0 skips the
+// timing and uses 4.
+// ===========================================================================
+
+namespace {
+
+struct TuneKey {
+  int W, H, n, viscous, pressure, storage, device;
+  bool operator<(const TuneKey& o) const {
+    return std::tie(W, H, n, viscous, pressure, storage, device) <
+           std::tie(o.W, o.H, o.n, o.viscous, o.pressure, o.storage, o.device);
+  }
+};
+std::map<TuneKey, int> g_tuned;
+std::mutex g_tune_mu;
+
+float time_steps(os_handle* t, float dt, int warm, int reps) {
+  if (os_update_async(t, nullptr, dt, warm, nullptr) != OS_OK) return -1.0f;
+  cudaEvent_t a = nullptr, b = nullptr;
+  if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) return -1.0f;
+  float ms = -1.0f;
+  cudaEventRecord(a, t->stream);
+  if (os_update_async(t, nullptr, dt, reps, nullptr) == OS_OK) {
+    cudaEventRecord(b, t->stream);
+    if (cudaEventSynchronize(b) != cudaSuccess || cudaEventElapsedTime(&ms, a, b) != cudaSuccess)
+      ms = -1.0f;
+  }
+  cudaStreamSynchronize(t->stream);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return ms;
+}
+
+int autotune_block_k(const os_config& base) {
+  constexpr int kDefault = 4;
+  const char* env = std::getenv("OPENSAYAL_GB300_AUTOTUNE");
+  if (env && env[0] == '0') return kDefault;
+  const TuneKey key{base.width, base.height, base.projection_n, base.viscosity != 0.0f,
+                    base.enable_pressure != 0, base.storage, base.device};
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    auto it = g_tuned.find(key);
+    if (it != g_tuned.end()) return it->second;
+  }
+  static const int kCandidates[] = {2, 4, 6, 8, 12};
+  const float dt = base.d_t > 0.0f ? base.d_t : 0.05f;
+  int best = kDefault;
+  float best_ms = 0.0f;
+  for (int K : kCandidates) {
+    if (K > std::max(1, base.projection_n)) break;
+    os_config c = base;
+    c.projection_block = K;
+    os_handle* t = nullptr;
+    if (os_create(&c, &t) != OS_OK) continue;  // e.g. out of memory: skip
+    const float ms = time_steps(t, dt, 2, 3);
+    os_destroy(t);
+    if (ms > 0.0f && (best_ms == 0.0f || ms < best_ms)) {
+      best_ms = ms;
+      best = K;
+    }
+  }
+  g_err[0] = '\0';  // a candidate that failed is not the caller's error
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  g_tuned[key] = best;
+  return best;
+}
+
+}  // namespace
 
 // ===========================================================================
 // Allocation-free diffusion

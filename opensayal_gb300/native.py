@@ -94,7 +94,7 @@ class OsFieldsView(C.Structure):
         ("width", C.c_int32),
         ("height", C.c_int32),
         ("storage", C.c_int32),
-        ("reserved", C.c_int32),
+        ("projection_block", C.c_int32),
         ("vel_x", C.c_void_p),
         ("vel_y", C.c_void_p),
         ("smoke", C.c_void_p),
