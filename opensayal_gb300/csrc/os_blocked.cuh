@@ -55,18 +55,53 @@ __host__ __device__ inline size_t diffusion_smem(int RH) {
   return 2 * ((size_t)RH * kRegionW + kArrPad) * 4;
 }
 
-// Four consecutive cells (i..i+3) of logical row j, zero off the grid.
-// `vec` = rows start 16-byte aligned and i is a multiple of 4.
-__device__ __forceinline__ float4 load_quad(const float* __restrict__ f, int W, int H, int i,
-                                            int j, bool vec) {
+// Four consecutive stored values as FP32 (one vector load).
+__device__ __forceinline__ float4 vec4_to_f32(const float* p) {
+  return __ldg(reinterpret_cast<const float4*>(p));
+}
+__device__ __forceinline__ float4 vec4_to_f32(const __half* p) {
+  const uint2 r = __ldg(reinterpret_cast<const uint2*>(p));
+  const float2 a = __half22float2(*reinterpret_cast<const __half2*>(&r.x));
+  const float2 b = __half22float2(*reinterpret_cast<const __half2*>(&r.y));
+  return make_float4(a.x, a.y, b.x, b.y);
+}
+__device__ __forceinline__ float4 vec4_to_f32(const __nv_bfloat16* p) {
+  const uint2 r = __ldg(reinterpret_cast<const uint2*>(p));
+  const float2 a = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&r.x));
+  const float2 b = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&r.y));
+  return make_float4(a.x, a.y, b.x, b.y);
+}
+__device__ __forceinline__ void f32_to_vec4(float* p, float4 q) {
+  *reinterpret_cast<float4*>(p) = q;
+}
+__device__ __forceinline__ void f32_to_vec4(__half* p, float4 q) {
+  __half2 a = __floats2half2_rn(q.x, q.y), b = __floats2half2_rn(q.z, q.w);
+  uint2 r;
+  r.x = *reinterpret_cast<uint32_t*>(&a);
+  r.y = *reinterpret_cast<uint32_t*>(&b);
+  *reinterpret_cast<uint2*>(p) = r;
+}
+__device__ __forceinline__ void f32_to_vec4(__nv_bfloat16* p, float4 q) {
+  __nv_bfloat162 a = __floats2bfloat162_rn(q.x, q.y), b = __floats2bfloat162_rn(q.z, q.w);
+  uint2 r;
+  r.x = *reinterpret_cast<uint32_t*>(&a);
+  r.y = *reinterpret_cast<uint32_t*>(&b);
+  *reinterpret_cast<uint2*>(p) = r;
+}
+
+// Four consecutive cells (i..i+3) of logical row j as FP32, zero off the
+// grid. `vec` = rows start aligned to 4 elements and i is a multiple of 4.
+template <class S>
+__device__ __forceinline__ float4 load_quad(const S* __restrict__ f, int W, int H, int i, int j,
+                                            bool vec) {
   float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
   if (j < 0 || j >= H) return q;
   const int64_t row = (int64_t)(H - 1 - j) * W;
-  if (vec && i >= 0 && i + 3 < W) return __ldg(reinterpret_cast<const float4*>(f + row + i));
-  if (i >= 0 && i < W) q.x = __ldg(f + row + i);
-  if (i + 1 >= 0 && i + 1 < W) q.y = __ldg(f + row + i + 1);
-  if (i + 2 >= 0 && i + 2 < W) q.z = __ldg(f + row + i + 2);
-  if (i + 3 >= 0 && i + 3 < W) q.w = __ldg(f + row + i + 3);
+  if (vec && i >= 0 && i + 3 < W) return vec4_to_f32(f + row + i);
+  if (i >= 0 && i < W) q.x = ldg<float>(f + row + i);
+  if (i + 1 >= 0 && i + 1 < W) q.y = ldg<float>(f + row + i + 1);
+  if (i + 2 >= 0 && i + 2 < W) q.z = ldg<float>(f + row + i + 2);
+  if (i + 3 >= 0 && i + 3 < W) q.w = ldg<float>(f + row + i + 3);
   return q;
 }
 
@@ -82,17 +117,18 @@ __device__ __forceinline__ uint32_t load_quad_u8(const uint8_t* __restrict__ f, 
   return q;
 }
 
-__device__ __forceinline__ void store_quad(float* __restrict__ f, int W, int H, int i, int j,
+template <class S>
+__device__ __forceinline__ void store_quad(S* __restrict__ f, int W, int H, int i, int j,
                                            bool vec, float4 q) {
   const int64_t row = (int64_t)(H - 1 - j) * W;
   if (vec && i + 3 < W) {
-    *reinterpret_cast<float4*>(f + row + i) = q;
+    f32_to_vec4(f + row + i, q);
     return;
   }
-  if (i < W) f[row + i] = q.x;
-  if (i + 1 < W) f[row + i + 1] = q.y;
-  if (i + 2 < W) f[row + i + 2] = q.z;
-  if (i + 3 < W) f[row + i + 3] = q.w;
+  if (i < W) st(f + row + i, q.x);
+  if (i + 1 < W) st(f + row + i + 1, q.y);
+  if (i + 2 < W) st(f + row + i + 2, q.z);
+  if (i + 3 < W) st(f + row + i + 3, q.w);
 }
 
 // ---------------------------------------------------------------------------
@@ -230,10 +266,10 @@ __device__ __forceinline__ void proj_half_sweep(float* __restrict__ S,
 // src/fluid.cu:203-219) as it loads; later passes continue the accumulation.
 // p is staged for owned cells only (halo pressure is never needed), so no CTA
 // reads pressure that another CTA writes in the same pass.
-template <bool PRESSURE>
+template <bool PRESSURE, class S>
 __global__ void __launch_bounds__(kBlockThreads, 1)
-k_project_blocked(const float* __restrict__ u_in, const float* __restrict__ v_in,
-                  float* __restrict__ u_out, float* __restrict__ v_out, float* __restrict__ p,
+k_project_blocked(const S* __restrict__ u_in, const S* __restrict__ v_in,
+                  S* __restrict__ u_out, S* __restrict__ v_out, float* __restrict__ p,
                   const uint8_t* __restrict__ fl, Consts c, const StepParams* __restrict__ prm,
                   int sweeps, int halo, int TX, int TY, int tiles_x, int zero_pressure) {
   extern __shared__ __align__(16) float smem[];
@@ -318,8 +354,8 @@ k_project_blocked(const float* __restrict__ u_in, const float* __restrict__ v_in
       if (xd < halo || xd >= halo + TX || i + d >= W) continue;
       const int64_t gk = cell_index(W, H, i + d, j);
       const int sd = y * kHalfW + (xd >> 1);
-      u_out[gk] = (xd & 1) ? P.uo[sd] : P.ue[sd];
-      v_out[gk] = (xd & 1) ? P.vo[sd] : P.ve[sd];
+      st(u_out + gk, (xd & 1) ? P.uo[sd] : P.ue[sd]);
+      st(v_out + gk, (xd & 1) ? P.vo[sd] : P.ve[sd]);
       if (PRESSURE) p[gk] = (xd & 1) ? P.po[sd] : P.pe[sd];
     }
   }
@@ -328,8 +364,9 @@ k_project_blocked(const float* __restrict__ u_in, const float* __restrict__ v_in
 // ---------------------------------------------------------------------------
 // Blocked Jacobi diffusion of u.
 // ---------------------------------------------------------------------------
+template <class S>
 __global__ void __launch_bounds__(kBlockThreads, 1)
-k_diffuse_blocked(const float* __restrict__ u_in, float* __restrict__ u_out, Consts c,
+k_diffuse_blocked(const S* __restrict__ u_in, S* __restrict__ u_out, Consts c,
                   const StepParams* __restrict__ prm, int sweeps, int halo, int TX, int TY,
                   int tiles_x) {
   extern __shared__ __align__(16) float smem[];
@@ -406,7 +443,7 @@ k_diffuse_blocked(const float* __restrict__ u_in, float* __restrict__ u_out, Con
     }
     for (int d = 0; d < 4; d++) {
       if (x + d < halo || x + d >= halo + TX || i + d >= W) continue;
-      u_out[cell_index(W, H, i + d, j)] = src[d];
+      st(u_out + cell_index(W, H, i + d, j), src[d]);
     }
   }
 }
@@ -447,9 +484,14 @@ inline int choose_block_k(const os_handle* h) {
   return 0;
 }
 
+// FP32 arithmetic on FP32, FP16 or BF16 storage. With reduced storage a value
+// is rounded to storage once per pass (the region stays FP32 in shared
+// memory), not once per sweep as in the plain kernels.
 template <class S, class A>
 inline bool blocked_supported(const os_handle*) {
-  return std::is_same<S, float>::value && std::is_same<A, float>::value;
+  return std::is_same<A, float>::value &&
+         (std::is_same<S, float>::value || std::is_same<S, __half>::value ||
+          std::is_same<S, __nv_bfloat16>::value);
 }
 
 inline int sm_count(int device) {
@@ -463,31 +505,32 @@ inline int sm_count(int device) {
 // (u, v) and writes the other. `cur_u`/`cur_v` track which copy holds the
 // live field (0: u/v, 1: ub/vb) and are updated for the caller.
 // `zero_first`: the first pass also performs zero_pressure (inside a step).
-inline int enqueue_blocked_projection_f32(os_handle* h, cudaStream_t st, int* cur_u, int* cur_v,
-                                          bool zero_first) {
+template <class S>
+inline int enqueue_blocked_projection(os_handle* h, cudaStream_t st, int* cur_u, int* cur_v,
+                                      bool zero_first) {
   const int K = h->block_k;
   const bool pressure = h->cfg.enable_pressure != 0;
   const TileGeom g = make_geom(h->W, h->H, 2 * K, true, pressure, sm_count(h->cfg.device));
-  float* U[2] = {static_cast<float*>(h->u), static_cast<float*>(h->ub)};
-  float* V[2] = {static_cast<float*>(h->v), static_cast<float*>(h->vb)};
+  S* U[2] = {static_cast<S*>(h->u), static_cast<S*>(h->ub)};
+  S* V[2] = {static_cast<S*>(h->v), static_cast<S*>(h->vb)};
   const int tiles = g.tiles_x * g.tiles_y;
   int launches = 0;
   for (int done = 0, pass = 0; done < h->c.n; pass++) {
     const int sweeps = std::min(K, h->c.n - done);
-    const float* uin = U[*cur_u];
-    const float* vin = V[*cur_v];
-    float* uout = U[1 - *cur_u];
-    float* vout = V[1 - *cur_v];
+    const S* uin = U[*cur_u];
+    const S* vin = V[*cur_v];
+    S* uout = U[1 - *cur_u];
+    S* vout = V[1 - *cur_v];
     if (pressure) {
-      cudaFuncSetAttribute(k_project_blocked<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)g.smem);
-      k_project_blocked<true><<<tiles, kBlockThreads, g.smem, st>>>(
+      cudaFuncSetAttribute(k_project_blocked<true, S>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.smem);
+      k_project_blocked<true, S><<<tiles, kBlockThreads, g.smem, st>>>(
           uin, vin, uout, vout, h->p, h->flags, h->c, h->d_params, sweeps, g.halo, g.TX, g.TY,
           g.tiles_x, (zero_first && pass == 0) ? 1 : 0);
     } else {
-      cudaFuncSetAttribute(k_project_blocked<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)g.smem);
-      k_project_blocked<false><<<tiles, kBlockThreads, g.smem, st>>>(
+      cudaFuncSetAttribute(k_project_blocked<false, S>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.smem);
+      k_project_blocked<false, S><<<tiles, kBlockThreads, g.smem, st>>>(
           uin, vin, uout, vout, h->p, h->flags, h->c, h->d_params, sweeps, g.halo, g.TX, g.TY,
           g.tiles_x, 0);
     }
@@ -499,17 +542,18 @@ inline int enqueue_blocked_projection_f32(os_handle* h, cudaStream_t st, int* cu
   return launches;
 }
 
-inline int enqueue_blocked_diffusion_f32(os_handle* h, cudaStream_t st, int* cur_u) {
+template <class S>
+inline int enqueue_blocked_diffusion(os_handle* h, cudaStream_t st, int* cur_u) {
   const int K = h->block_k;
   const TileGeom g = make_geom(h->W, h->H, K, false, false, sm_count(h->cfg.device));
-  float* U[2] = {static_cast<float*>(h->u), static_cast<float*>(h->ub)};
+  S* U[2] = {static_cast<S*>(h->u), static_cast<S*>(h->ub)};
   const int tiles = g.tiles_x * g.tiles_y;
-  cudaFuncSetAttribute(k_diffuse_blocked, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaFuncSetAttribute(k_diffuse_blocked<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)g.smem);
   int launches = 0;
   for (int done = 0; done < h->c.n;) {
     const int sweeps = std::min(K, h->c.n - done);
-    k_diffuse_blocked<<<tiles, kBlockThreads, g.smem, st>>>(
+    k_diffuse_blocked<S><<<tiles, kBlockThreads, g.smem, st>>>(
         U[*cur_u], U[1 - *cur_u], h->c, h->d_params, sweeps, g.halo, g.TX, g.TY, g.tiles_x);
     launches++;
     *cur_u = 1 - *cur_u;

@@ -132,10 +132,17 @@ bool use_blocked(const os_handle* h) {
 }
 
 template <class S, class A>
+constexpr bool kBlockedTypes = std::is_same<A, float>::value &&
+                               (std::is_same<S, float>::value || std::is_same<S, __half>::value ||
+                                std::is_same<S, __nv_bfloat16>::value);
+
+template <class S, class A>
 void enqueue_diffusion(os_handle* h, Vel<S>& w, Enq& q) {
-  if (use_blocked<S, A>(h)) {
-    q.count += enqueue_blocked_diffusion_f32(h, q.st, &w.cu);
-    return;
+  if constexpr (kBlockedTypes<S, A>) {
+    if (use_blocked<S, A>(h)) {
+      q.count += enqueue_blocked_diffusion<S>(h, q.st, &w.cu);
+      return;
+    }
   }
   const dim3 g2((h->W + 127) / 128, h->H);
   for (int t = 0; t < h->c.n; t++) {
@@ -147,9 +154,11 @@ void enqueue_diffusion(os_handle* h, Vel<S>& w, Enq& q) {
 
 template <class S, class A>
 void enqueue_projection(os_handle* h, Vel<S>& w, Enq& q, bool zero_pressure_first) {
-  if (use_blocked<S, A>(h)) {
-    q.count += enqueue_blocked_projection_f32(h, q.st, &w.cu, &w.cv, zero_pressure_first);
-    return;
+  if constexpr (kBlockedTypes<S, A>) {
+    if (use_blocked<S, A>(h)) {
+      q.count += enqueue_blocked_projection<S>(h, q.st, &w.cu, &w.cv, zero_pressure_first);
+      return;
+    }
   }
   const dim3 gp(((h->W + 1) / 2 + 127) / 128, h->H);
   for (int t = 0; t < h->c.n; t++) {
@@ -598,7 +607,7 @@ int os_create(const os_config* cfg, os_handle** out) {
       (e = cudaStreamSynchronize(h->stream)) != cudaSuccess)
     return fail(set_err(OS_ERR_CUDA, "init: %s", cudaGetErrorString(e)));
   if (h->block_k == 0)
-    h->block_k = h->storage == OS_STORAGE_F32 ? autotune_block_k(*cfg) : -1;
+    h->block_k = h->storage != OS_STORAGE_F64 ? autotune_block_k(*cfg) : -1;
   *out = h;
   return OS_OK;
 }

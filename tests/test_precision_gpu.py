@@ -1,0 +1,81 @@
+"""Storage precision against an FP64 run of the same scheme.
+
+The FP64 run (storage OS_STORAGE_F64) uses the same kernels in double with
+IEEE division. Errors grow with steps because the wake behind the obstacle
+amplifies small differences: FP32 (the reference's precision) reaches ~1-2e-3
+relative L2 after 1000 steps of the 256x128 case, FP16 storage ~0.06-0.1 and
+BF16 storage ~0.3-0.8. These tests pin the ordering and bounds at 100 steps.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from opensayal_gb300 import native, scenarios
+from opensayal_gb300.fluid import Fluid
+from tests.parity_cases import perturbed_state
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ("vel_x", "vel_y", "smoke")
+
+
+def run(cfg, storage, steps, state, block=0):
+    c = cfg.copy()
+    c.storage = storage
+    c.projection_block = block
+    with Fluid(c) as f:
+        for k, a in state.items():
+            f.upload(k, a)
+        f.update_async(None, c.d_t, steps)
+        f.synchronize()
+        return {k: f.download(k) for k in FIELDS}
+
+
+@pytest.fixture(scope="module")
+def small_runs():
+    cfg = scenarios.small_config()
+    state = perturbed_state(cfg, 1)
+    steps = 100
+    ref = run(cfg, native.STORAGE_F64, steps, state)
+    return cfg, state, steps, ref
+
+
+def errors(out, ref):
+    return {k: oracle.rel_l2(out[k], ref[k]) for k in FIELDS}
+
+
+def test_fp32_against_fp64(gpu, small_runs):
+    cfg, state, steps, ref = small_runs
+    e = errors(run(cfg, native.STORAGE_F32, steps, state), ref)
+    assert max(e.values()) < 1e-3, e
+
+
+def test_reduced_storage_against_fp64(gpu, small_runs):
+    cfg, state, steps, ref = small_runs
+    e32 = max(errors(run(cfg, native.STORAGE_F32, steps, state), ref).values())
+    e16 = max(errors(run(cfg, native.STORAGE_F16, steps, state), ref).values())
+    eb16 = max(errors(run(cfg, native.STORAGE_BF16, steps, state), ref).values())
+    assert e32 < e16 < eb16, (e32, e16, eb16)
+    assert e16 < 0.05 and eb16 < 0.5, (e16, eb16)
+
+
+@pytest.mark.parametrize("storage", [native.STORAGE_F16, native.STORAGE_BF16])
+def test_reduced_storage_blocked_is_no_worse_than_plain(gpu, small_runs, storage):
+    """The blocked engine rounds to storage once per pass instead of once per
+    sweep, so its error against FP64 must not exceed the plain kernels'."""
+    cfg, state, steps, ref = small_runs
+    blocked = max(errors(run(cfg, storage, steps, state, block=8), ref).values())
+    plain = max(errors(run(cfg, storage, steps, state, block=-1), ref).values())
+    assert blocked <= plain * 1.05, (blocked, plain)
+
+
+def test_downloads_convert_storage_to_fp32(gpu):
+    cfg = scenarios.small_config()
+    for storage, tol in ((native.STORAGE_F16, 2 ** -11), (native.STORAGE_BF16, 2 ** -8)):
+        c = cfg.copy()
+        c.storage = storage
+        with Fluid(c) as f:
+            x = np.linspace(-3, 3, c.width * c.height).astype(np.float32)
+            f.upload("vel_x", x)
+            y = f.download("vel_x")
+            assert np.all(np.abs(y - x) <= tol * np.abs(x) + 1e-7)
