@@ -255,6 +255,39 @@ int os_profile_phase(os_handle* h, int32_t phase, const os_source* src, float dt
  */
 int os_diffuse_noalloc(const os_config* cfg, float* u, float dt, void* stream);
 
+/*
+ * Batched scenarios: many independent tunnels of different sizes advanced
+ * together, one CUDA graph per step and one persistent kernel per phase that
+ * walks a work list of rows or tiles across all scenarios. No reference
+ * counterpart (the reference runs one grid). Each scenario advances exactly as
+ * a single handle with the same sweeps-per-pass would: the same per-cell and
+ * per-tile code runs, only the schedule differs. Scenarios are FP32 with
+ * pressure off, on one device; each keeps its own fields, reachable through
+ * os_batch_scenario() with the single-handle calls (upload, download, fields).
+ */
+typedef struct os_batch os_batch;
+
+typedef struct os_batch_stats {
+  int32_t scenarios;
+  int32_t block_k;            /* sweeps per blocked pass */
+  int32_t kernels_per_step;   /* launches in one step's graph */
+  int32_t reserved;
+  int64_t cells;              /* total cells over all scenarios */
+  int64_t launches;           /* kernels launched by os_batch_step so far */
+  int64_t tile_items_per_step;
+} os_batch_stats;
+
+/* `block_k`: sweeps per blocked pass for every scenario (0 = 8). */
+int os_batch_create(const os_config* cfgs, int32_t count, int32_t block_k, os_batch** out);
+int os_batch_destroy(os_batch* b);
+/* `steps` steps of every scenario (graph replays) enqueued on `stream` (NULL:
+ * the batch's own stream); each scenario uses its own config's d_t. */
+int os_batch_step(os_batch* b, int32_t steps, void* stream);
+int os_batch_synchronize(os_batch* b);
+/* The handle of scenario `index`, owned by the batch (do not destroy it). */
+int os_batch_scenario(os_batch* b, int32_t index, os_handle** out);
+int os_batch_info(os_batch* b, os_batch_stats* out);
+
 #ifdef __cplusplus
 }  /* extern "C" */
 #endif

@@ -266,16 +266,17 @@ __device__ __forceinline__ void proj_half_sweep(float* __restrict__ S,
 // src/fluid.cu:203-219) as it loads; later passes continue the accumulation.
 // p is staged for owned cells only (halo pressure is never needed), so no CTA
 // reads pressure that another CTA writes in the same pass.
+// One tile (tx, ty) of one grid: stage, `sweeps` red/black sweeps, write back.
 template <bool PRESSURE, class S>
-__global__ void __launch_bounds__(kBlockThreads, 1)
-k_project_blocked(const S* __restrict__ u_in, const S* __restrict__ v_in,
-                  S* __restrict__ u_out, S* __restrict__ v_out, float* __restrict__ p,
-                  const uint8_t* __restrict__ fl, Consts c, const StepParams* __restrict__ prm,
-                  int sweeps, int halo, int TX, int TY, int tiles_x, int zero_pressure) {
-  extern __shared__ __align__(16) float smem[];
+__device__ __forceinline__ void project_tile(float* smem, int tx, int ty,
+                                             const S* __restrict__ u_in,
+                                             const S* __restrict__ v_in, S* __restrict__ u_out,
+                                             S* __restrict__ v_out, float* __restrict__ p,
+                                             const uint8_t* __restrict__ fl, const Consts& c,
+                                             const StepParams* __restrict__ prm, int sweeps,
+                                             int halo, int TX, int TY, int zero_pressure) {
   const int RH = TY + 2 * halo;
   const ProjPlanes P = proj_planes<PRESSURE>(smem, RH);
-  const int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
   const int gx0 = tx * TX - halo, gy0 = ty * TY - halo;
   const int W = c.W, H = c.H;
   const bool vec = ((W & 3) == 0) && ((gx0 & 3) == 0);
@@ -361,19 +362,28 @@ k_project_blocked(const S* __restrict__ u_in, const S* __restrict__ v_in,
   }
 }
 
+template <bool PRESSURE, class S>
+__global__ void __launch_bounds__(kBlockThreads, 1)
+k_project_blocked(const S* __restrict__ u_in, const S* __restrict__ v_in,
+                  S* __restrict__ u_out, S* __restrict__ v_out, float* __restrict__ p,
+                  const uint8_t* __restrict__ fl, Consts c, const StepParams* __restrict__ prm,
+                  int sweeps, int halo, int TX, int TY, int tiles_x, int zero_pressure) {
+  extern __shared__ __align__(16) float smem[];
+  project_tile<PRESSURE, S>(smem, blockIdx.x % tiles_x, blockIdx.x / tiles_x, u_in, v_in, u_out,
+                            v_out, p, fl, c, prm, sweeps, halo, TX, TY, zero_pressure);
+}
+
 // ---------------------------------------------------------------------------
 // Blocked Jacobi diffusion of u.
 // ---------------------------------------------------------------------------
 template <class S>
-__global__ void __launch_bounds__(kBlockThreads, 1)
-k_diffuse_blocked(const S* __restrict__ u_in, S* __restrict__ u_out, Consts c,
-                  const StepParams* __restrict__ prm, int sweeps, int halo, int TX, int TY,
-                  int tiles_x) {
-  extern __shared__ __align__(16) float smem[];
+__device__ __forceinline__ void diffuse_tile(float* smem, int tx, int ty,
+                                             const S* __restrict__ u_in, S* __restrict__ u_out,
+                                             const Consts& c, const StepParams* __restrict__ prm,
+                                             int sweeps, int halo, int TX, int TY) {
   const int RH = TY + 2 * halo;
   float* A = smem;
   float* B = smem + RH * kRegionW + kArrPad;
-  const int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
   const int gx0 = tx * TX - halo, gy0 = ty * TY - halo;
   const int W = c.W, H = c.H;
   const bool vec = ((W & 3) == 0) && ((gx0 & 3) == 0);
@@ -422,7 +432,7 @@ k_diffuse_blocked(const S* __restrict__ u_in, S* __restrict__ u_out, Consts c,
         const int e = y * kRegionW + x;
         const float up = A[e + kRegionW];
         // src/fluid.cu:178-182: neighbours (i-1, j), (i+1, j), (i, j-1), (i, j+1)
-        B[e] = (centre + a * (A[e - 1] + A[e + 1] + down + up)) / (1 + 4 * a);
+        B[e] = fma_rn(a, A[e - 1] + A[e + 1] + down + up, centre) / fma_rn(4.0f, a, 1.0f);
         down = centre;
         centre = up;
       }
@@ -446,6 +456,16 @@ k_diffuse_blocked(const S* __restrict__ u_in, S* __restrict__ u_out, Consts c,
       st(u_out + cell_index(W, H, i + d, j), src[d]);
     }
   }
+}
+
+template <class S>
+__global__ void __launch_bounds__(kBlockThreads, 1)
+k_diffuse_blocked(const S* __restrict__ u_in, S* __restrict__ u_out, Consts c,
+                  const StepParams* __restrict__ prm, int sweeps, int halo, int TX, int TY,
+                  int tiles_x) {
+  extern __shared__ __align__(16) float smem[];
+  diffuse_tile<S>(smem, blockIdx.x % tiles_x, blockIdx.x / tiles_x, u_in, u_out, c, prm, sweeps,
+                  halo, TX, TY);
 }
 
 // ---------------------------------------------------------------------------

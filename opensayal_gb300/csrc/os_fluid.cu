@@ -966,3 +966,254 @@ extern "C" int os_diffuse_noalloc(const os_config* cfg, float* u, float dt, void
   CUDA_OR_RETURN(cudaGetLastError());
   return OS_OK;
 }
+
+// ===========================================================================
+// Batched scenarios (os_batch_*)
+// ===========================================================================
+
+#include "os_batch.cuh"
+
+struct os_batch {
+  std::vector<os_handle*> handles;
+  int K = 8;
+  int device = 0;
+  int sms = 152;
+  cudaStream_t stream = nullptr;
+  ScenarioDesc* d_table = nullptr;
+  RowItem* d_rows = nullptr;
+  TileItem* d_tiles = nullptr;
+  int n_rows = 0;
+  std::vector<int> diff_off, diff_cnt, proj_off, proj_cnt;
+  TileGeom gd{}, gp{};
+  cudaGraphExec_t graph = nullptr;
+  int kernels_per_step = 0;
+  int64_t launches = 0;
+  int64_t cells = 0;
+};
+
+namespace {
+
+// Largest even tile height whose region fits shared memory.
+TileGeom batch_geom(int halo, bool projection) {
+  TileGeom g{};
+  g.halo = halo;
+  g.TX = kRegionW - 2 * halo;
+  int TY = 2;
+  while (true) {
+    const int next = TY + 2;
+    const size_t sm = projection ? projection_smem(next + 2 * halo, false)
+                                 : diffusion_smem(next + 2 * halo);
+    if (sm > kMaxSmem) break;
+    TY = next;
+  }
+  g.TY = TY;
+  g.RH = TY + 2 * halo;
+  g.smem = projection ? projection_smem(g.RH, false) : diffusion_smem(g.RH);
+  return g;
+}
+
+void free_batch(os_batch* b) {
+  if (!b) return;
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  if (b->d_table) cudaFree(b->d_table);
+  if (b->d_rows) cudaFree(b->d_rows);
+  if (b->d_tiles) cudaFree(b->d_tiles);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  for (os_handle* h : b->handles) os_destroy(h);
+  delete b;
+}
+
+int build_batch_graph(os_batch* b) {
+  cudaStream_t st = b->stream;
+  const int count = (int)b->handles.size();
+  int kernels = 0;
+  CUDA_OR_RETURN(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  const int row_grid = std::min(b->n_rows, b->sms * 16);
+  k_batch_forces<<<row_grid, 128, 0, st>>>(b->d_rows, b->n_rows, b->d_table);
+  kernels++;
+  for (size_t p = 0; p < b->diff_cnt.size(); p++) {
+    const int cnt = b->diff_cnt[p];
+    k_batch_diffuse<<<std::min(cnt, b->sms), kBlockThreads, b->gd.smem, st>>>(
+        b->d_tiles + b->diff_off[p], cnt, b->d_table, (int)p, b->K, b->gd.halo, b->gd.TX,
+        b->gd.TY);
+    kernels++;
+  }
+  for (size_t p = 0; p < b->proj_cnt.size(); p++) {
+    const int cnt = b->proj_cnt[p];
+    k_batch_project<<<std::min(cnt, b->sms), kBlockThreads, b->gp.smem, st>>>(
+        b->d_tiles + b->proj_off[p], cnt, b->d_table, (int)p, b->K, b->gp.halo, b->gp.TX,
+        b->gp.TY);
+    kernels++;
+  }
+  k_batch_extrapolate<<<std::min(count, b->sms * 4), 1024, 0, st>>>(b->d_table, count);
+  k_batch_advect_velocity<<<row_grid, 128, 0, st>>>(b->d_rows, b->n_rows, b->d_table);
+  k_batch_advect_smoke<<<row_grid, 128, 0, st>>>(b->d_rows, b->n_rows, b->d_table);
+  k_batch_finish_smoke<<<row_grid, 128, 0, st>>>(b->d_rows, b->n_rows, b->d_table);
+  kernels += 4;
+  const cudaError_t le = cudaGetLastError();
+  cudaGraph_t g = nullptr;
+  const cudaError_t ce = cudaStreamEndCapture(st, &g);
+  if (le != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    return set_err(OS_ERR_CUDA, "batch launch: %s", cudaGetErrorString(le));
+  }
+  if (ce != cudaSuccess) return set_err(OS_ERR_CUDA, "batch capture: %s", cudaGetErrorString(ce));
+  const cudaError_t ie = cudaGraphInstantiate(&b->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (ie != cudaSuccess) return set_err(OS_ERR_CUDA, "batch instantiate: %s", cudaGetErrorString(ie));
+  b->kernels_per_step = kernels;
+  return OS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int os_batch_create(const os_config* cfgs, int32_t count, int32_t block_k, os_batch** out) {
+  if (!cfgs || !out || count < 1) return set_err(OS_ERR_INVALID, "bad argument");
+  *out = nullptr;
+  const int K = block_k > 0 ? std::min(block_k, 16) : 8;
+  for (int i = 0; i < count; i++) {
+    const os_config& c = cfgs[i];
+    int rc = validate(&c);
+    if (rc) return rc;
+    if (c.storage != OS_STORAGE_F32 || c.enable_pressure || c.device != cfgs[0].device)
+      return set_err(OS_ERR_UNSUPPORTED,
+                     "batched scenarios are FP32, pressure off, on one device (scenario %d)", i);
+  }
+  os_batch* b = new (std::nothrow) os_batch();
+  if (!b) return set_err(OS_ERR_NOMEM, "host allocation failed");
+  b->K = K;
+  b->device = cfgs[0].device;
+  b->sms = sm_count(b->device);
+  auto fail = [&](int code) {
+    free_batch(b);
+    return code;
+  };
+  cudaError_t e = cudaSetDevice(b->device);
+  if (e != cudaSuccess) return fail(set_err(OS_ERR_CUDA, "cudaSetDevice: %s", cudaGetErrorString(e)));
+  if ((e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking)) != cudaSuccess)
+    return fail(set_err(OS_ERR_CUDA, "stream: %s", cudaGetErrorString(e)));
+  b->gd = batch_geom(K, false);
+  b->gp = batch_geom(2 * K, true);
+  std::vector<ScenarioDesc> table;
+  std::vector<RowItem> rows;
+  for (int i = 0; i < count; i++) {
+    os_config c = cfgs[i];
+    c.projection_block = K;
+    os_handle* h = nullptr;
+    int rc = os_create(&c, &h);
+    if (rc) return fail(rc);
+    b->handles.push_back(h);
+    if ((rc = push_params(h, nullptr, c.d_t, h->stream))) return fail(rc);
+    ScenarioDesc d{};
+    d.c = h->c;
+    d.smoke_period = h->smoke_period;
+    d.smoke_on = c.enable_smoke && c.tunnel_smoke != 0.0f;
+    d.proj_passes = (h->c.n + K - 1) / K;
+    d.diff_passes = c.viscosity != 0.0f ? d.proj_passes : 0;
+    d.prm = h->d_params;
+    d.u = static_cast<float*>(h->u);
+    d.v = static_cast<float*>(h->v);
+    d.ub = static_cast<float*>(h->ub);
+    d.vb = static_cast<float*>(h->vb);
+    d.s = static_cast<float*>(h->s);
+    d.sb = static_cast<float*>(h->sb);
+    d.flags = h->flags;
+    table.push_back(d);
+    for (int j = 0; j < h->H; j++) rows.push_back(RowItem{i, j});
+    b->cells += (int64_t)h->N;
+  }
+  // Tile lists: pass p of a phase lists the tiles of every scenario that
+  // still has a pass p to do.
+  std::vector<TileItem> tiles;
+  auto add_passes = [&](const TileGeom& g, bool diffusion, std::vector<int>& off,
+                        std::vector<int>& cnt) {
+    int max_passes = 0;
+    for (const ScenarioDesc& d : table)
+      max_passes = std::max(max_passes, diffusion ? d.diff_passes : d.proj_passes);
+    for (int p = 0; p < max_passes; p++) {
+      off.push_back((int)tiles.size());
+      for (int s = 0; s < count; s++) {
+        const ScenarioDesc& d = table[s];
+        if ((diffusion ? d.diff_passes : d.proj_passes) <= p) continue;
+        const int tx_n = (d.c.W + g.TX - 1) / g.TX, ty_n = (d.c.H + g.TY - 1) / g.TY;
+        for (int ty = 0; ty < ty_n; ty++)
+          for (int tx = 0; tx < tx_n; tx++) tiles.push_back(TileItem{s, tx, ty});
+      }
+      cnt.push_back((int)tiles.size() - off.back());
+    }
+  };
+  add_passes(b->gd, true, b->diff_off, b->diff_cnt);
+  add_passes(b->gp, false, b->proj_off, b->proj_cnt);
+  b->n_rows = (int)rows.size();
+  if ((e = cudaMalloc(&b->d_table, table.size() * sizeof(ScenarioDesc))) != cudaSuccess ||
+      (e = cudaMalloc(&b->d_rows, rows.size() * sizeof(RowItem))) != cudaSuccess ||
+      (e = cudaMalloc(&b->d_tiles, std::max<size_t>(1, tiles.size()) * sizeof(TileItem))) !=
+          cudaSuccess)
+    return fail(set_err(OS_ERR_NOMEM, "batch tables: %s", cudaGetErrorString(e)));
+  cudaMemcpy(b->d_table, table.data(), table.size() * sizeof(ScenarioDesc), cudaMemcpyHostToDevice);
+  cudaMemcpy(b->d_rows, rows.data(), rows.size() * sizeof(RowItem), cudaMemcpyHostToDevice);
+  if (!tiles.empty())
+    cudaMemcpy(b->d_tiles, tiles.data(), tiles.size() * sizeof(TileItem), cudaMemcpyHostToDevice);
+  for (os_handle* h : b->handles) cudaStreamSynchronize(h->stream);
+  cudaFuncSetAttribute(k_batch_diffuse, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)b->gd.smem);
+  cudaFuncSetAttribute(k_batch_project, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)b->gp.smem);
+  if ((e = cudaDeviceSynchronize()) != cudaSuccess)
+    return fail(set_err(OS_ERR_CUDA, "batch set-up: %s", cudaGetErrorString(e)));
+  int rc = build_batch_graph(b);
+  if (rc) return fail(rc);
+  *out = b;
+  return OS_OK;
+}
+
+int os_batch_destroy(os_batch* b) {
+  if (!b) return OS_OK;
+  cudaSetDevice(b->device);
+  cudaStreamSynchronize(b->stream);
+  free_batch(b);
+  return OS_OK;
+}
+
+int os_batch_step(os_batch* b, int32_t steps, void* stream) {
+  if (!b || steps < 0) return set_err(OS_ERR_INVALID, "bad argument");
+  int cur = -1;
+  CUDA_OR_RETURN(cudaGetDevice(&cur));
+  if (cur != b->device) CUDA_OR_RETURN(cudaSetDevice(b->device));
+  cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : b->stream;
+  for (int t = 0; t < steps; t++) CUDA_OR_RETURN(cudaGraphLaunch(b->graph, st));
+  b->launches += (int64_t)steps * b->kernels_per_step;
+  return OS_OK;
+}
+
+int os_batch_synchronize(os_batch* b) {
+  if (!b) return set_err(OS_ERR_INVALID, "null batch");
+  CUDA_OR_RETURN(cudaStreamSynchronize(b->stream));
+  return OS_OK;
+}
+
+int os_batch_scenario(os_batch* b, int32_t index, os_handle** out) {
+  if (!b || !out || index < 0 || index >= (int)b->handles.size())
+    return set_err(OS_ERR_INVALID, "bad scenario index");
+  *out = b->handles[index];
+  return OS_OK;
+}
+
+int os_batch_info(os_batch* b, os_batch_stats* out) {
+  if (!b || !out) return set_err(OS_ERR_INVALID, "null argument");
+  memset(out, 0, sizeof *out);
+  out->scenarios = (int32_t)b->handles.size();
+  out->block_k = b->K;
+  out->kernels_per_step = b->kernels_per_step;
+  out->cells = b->cells;
+  out->launches = b->launches;
+  int64_t tiles = 0;
+  for (int c : b->diff_cnt) tiles += c;
+  for (int c : b->proj_cnt) tiles += c;
+  out->tile_items_per_step = tiles;
+  return OS_OK;
+}
+
+}  // extern "C"

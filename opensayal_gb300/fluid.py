@@ -143,16 +143,32 @@ class Fluid:
         h = C.c_void_p()
         check(self._lib.os_create(C.byref(self.config), C.byref(h)))
         self._h = h
+        self._owned = True
+        self._set_shape(config)
+
+    def _set_shape(self, config: OsConfig) -> None:
         self.width = config.width
         self.height = config.height
         self.n = config.projection_n
         self.o = config.projection_o
         self.cell_size = int(config.cell_size)
 
+    @classmethod
+    def view(cls, handle: C.c_void_p, config: OsConfig) -> "Fluid":
+        """A Fluid over a handle owned elsewhere (a batch scenario)."""
+        f = cls.__new__(cls)
+        f._lib = native.load()
+        f.config = config.copy()
+        f._h = C.c_void_p(handle.value)
+        f._owned = False
+        f._set_shape(config)
+        return f
+
     # -- lifecycle -----------------------------------------------------------
     def close(self) -> None:
         if getattr(self, "_h", None) is not None and self._h.value:
-            check(self._lib.os_destroy(self._h))
+            if self._owned:
+                check(self._lib.os_destroy(self._h))
             self._h = None
 
     def __del__(self):

@@ -124,7 +124,26 @@ SIGNATURES = [
                                    C.c_int32, C.c_void_p, C.POINTER(C.c_float),
                                    C.POINTER(C.c_int32)]),
     ("os_diffuse_noalloc", C.c_int, [C.POINTER(OsConfig), C.c_void_p, C.c_float, C.c_void_p]),
+    ("os_batch_create", C.c_int, [C.POINTER(OsConfig), C.c_int32, C.c_int32,
+                                  C.POINTER(C.c_void_p)]),
+    ("os_batch_destroy", C.c_int, [C.c_void_p]),
+    ("os_batch_step", C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
+    ("os_batch_synchronize", C.c_int, [C.c_void_p]),
+    ("os_batch_scenario", C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p)]),
+    ("os_batch_info", C.c_int, [C.c_void_p, C.c_void_p]),
 ]
+
+
+class OsBatchStats(C.Structure):
+    _fields_ = [
+        ("scenarios", C.c_int32),
+        ("block_k", C.c_int32),
+        ("kernels_per_step", C.c_int32),
+        ("reserved", C.c_int32),
+        ("cells", C.c_int64),
+        ("launches", C.c_int64),
+        ("tile_items_per_step", C.c_int64),
+    ]
 
 _lib = None
 
