@@ -136,6 +136,17 @@ def dist_max(world, x: float) -> float:
     return float(t.item())
 
 
+def dist_sum(world, x: float) -> float:
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if torch.cuda.is_available() and dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t)
+    return float(t.item())
+
+
 def cpu_baseline(cfg, budget_s: float = 15.0, max_steps: int = 400) -> dict:
     """The oracle port on the host cores (rank 0, N=1 only)."""
     import oracle
@@ -289,8 +300,10 @@ def run_batched(args, world, rank, local) -> dict | None:
     torch.cuda.set_device(local)
     count = args.scenarios
     cfgs = scenarios.batched_scenarios(count, seed=4 + 1000 * rank)
-    for c in cfgs:
+    for i, c in enumerate(cfgs):
         c.device = local
+        if args.mixed and i % 2:
+            c.storage = 2  # OS_STORAGE_BF16
     cells = sum(c.width * c.height for c in cfgs)
     b = Batch(cfgs, block_k=args.block if args.block and args.block > 0 else 0)
     for i, c in enumerate(cfgs):
@@ -351,9 +364,9 @@ def run_batched(args, world, rank, local) -> dict | None:
     res = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_s * 1e3 / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic",
-        "config": {"workload": f"batched: {count} uneven tunnels (seed 4), W,H in 128..1024 step "
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32/bf16" if args.mixed else "f32", "data": "synthetic",
+        "config": {"workload": f"batched{' mixed BF16/FP32' if args.mixed else ''}: {count} uneven tunnels (seed 4), W,H in 128..1024 step "
                                f"32, n in {{50,100,200}}, dt 0.05", "scenarios": count,
                    "cells": cells, "block_k": st.block_k, "kernels_per_step": st.kernels_per_step,
                    "tile_items_per_step": st.tile_items_per_step,
@@ -364,6 +377,64 @@ def run_batched(args, world, rank, local) -> dict | None:
         "gpu_launches": int(st.launches - launches0),
         "one_at_a_time": {"plain_per_sweep_sync": plain, "blocked_graph_sync": alone,
                           "unit": UNIT, "steps_per_scenario": 2},
+        "clocks": clk.summary(),
+    }
+    return res if rank == 0 else None
+
+
+def run_serving(args, world, rank, local) -> dict | None:
+    """Poisson arrivals (seed 5) of tunnels drawn as in the batched workload,
+    steps U[100, 5000], BF16 or FP32 storage (p = 0.5), served by continuous
+    batching within a device-memory budget; the same arrival trace served one
+    request at a time by single handles is the baseline. Both run to the same
+    horizon (arrival window plus a drain allowance)."""
+    import torch
+    from opensayal_gb300 import scenarios
+    from opensayal_gb300.build import build_library
+    from opensayal_gb300.serving import Server, serve_serial
+    build_library()
+    torch.cuda.set_device(local)
+    reqs = scenarios.serving_requests(args.serve_rate, args.serve_seconds, seed=5 + 1000 * rank)
+    for r in reqs:
+        r.config.device = local
+    horizon = args.serve_seconds + args.serve_drain
+    # Warm the library and the graph path on two small requests first.
+    warm = scenarios.serving_requests(1000.0, 0.002, seed=99)[:2]
+    for r in warm:
+        r.config.device = local
+        r.steps = 3
+    with Server(budget_bytes=1 << 30, block_k=8, max_members=2) as w:
+        w.run(warm, 60.0)
+    budget = int(args.serve_budget_gb * 1e9)
+    dist_barrier(world)
+    with Clocks(local) as clk:
+        with Server(budget_bytes=budget, block_k=8, max_members=args.serve_slots,
+                    chunk=args.serve_chunk) as srv:
+            rep = srv.run(reqs, horizon)
+            st = srv.batch.stats()
+    served = rep.summary()
+    serial = None
+    if not args.no_serial:
+        serial = serve_serial(reqs, horizon, block_k=8).summary()
+    value = dist_sum(world, float(rep.cell_steps)) / dist_max(world, rep.wall_s)
+    res = {
+        "metric": "served cell-steps/s (continuous batching, Poisson arrivals)",
+        "value": value, "unit": UNIT, "n_gpus": world, "steps": int(st.steps_enqueued),
+        "warmup": 1, "ms_per_step": rep.wall_s * 1e3 / max(1, st.steps_enqueued),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32/bf16",
+        "data": "synthetic",
+        "config": {"workload": f"serving: Poisson {args.serve_rate}/s for {args.serve_seconds} s "
+                               f"(seed 5), tunnels as batched, steps U[100,5000], BF16 p=0.5",
+                   "budget_gb": args.serve_budget_gb, "max_members": args.serve_slots,
+                   "chunk": args.serve_chunk, "horizon_s": horizon, "block_k": st.block_k,
+                   "l2": "inputs larger than L2 (tens of members, ~12 MB each)",
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "serving": served,
+        "serial_plain": serial,
+        "e2e": {"value": value, "unit": UNIT,
+                "h2d_bytes_per_step": rep.h2d_bytes // max(1, st.steps_enqueued),
+                "d2h_bytes_per_step": rep.d2h_bytes // max(1, st.steps_enqueued)},
+        "gpu_launches": int(st.launches),
         "clocks": clk.summary(),
     }
     return res if rank == 0 else None
@@ -442,11 +513,20 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="default",
-                    choices=["default", "small", "large", "batched"])
+                    choices=["default", "small", "large", "batched", "serving"])
     ap.add_argument("--scenarios", type=int, default=512, help="batched workload size")
     ap.add_argument("--block", type=int, default=None,
                     help="red/black sweeps per blocked pass (0 autotune, -1 plain)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--mixed", action="store_true",
+                    help="batched: BF16 storage for half of the scenarios")
+    ap.add_argument("--serve-rate", type=float, default=200.0)
+    ap.add_argument("--serve-seconds", type=float, default=60.0)
+    ap.add_argument("--serve-drain", type=float, default=30.0)
+    ap.add_argument("--serve-budget-gb", type=float, default=150.0)
+    ap.add_argument("--serve-slots", type=int, default=64)
+    ap.add_argument("--serve-chunk", type=int, default=2)
+    ap.add_argument("--no-serial", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -454,7 +534,8 @@ def main():
     if args.impl == "reference":
         res = run_reference(args, world, rank, local)
     else:
-        res = (run_batched if args.workload == "batched" else run_gb300)(args, world, rank, local)
+        runner = {"batched": run_batched, "serving": run_serving}.get(args.workload, run_gb300)
+        res = runner(args, world, rank, local)
     if res is not None:
         print(json.dumps(res), flush=True)
     if world > 1:

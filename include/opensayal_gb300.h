@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define OS_ABI_VERSION 1
+#define OS_ABI_VERSION 2
 
 typedef enum os_status {
   OS_OK = 0,
@@ -256,36 +256,79 @@ int os_profile_phase(os_handle* h, int32_t phase, const os_source* src, float dt
 int os_diffuse_noalloc(const os_config* cfg, float* u, float dt, void* stream);
 
 /*
- * Batched scenarios: many independent tunnels of different sizes advanced
- * together, one CUDA graph per step and one persistent kernel per phase that
- * walks a work list of rows or tiles across all scenarios. No reference
- * counterpart (the reference runs one grid). Each scenario advances exactly as
- * a single handle with the same sweeps-per-pass would: the same per-cell and
- * per-tile code runs, only the schedule differs. Scenarios are FP32 with
- * pressure off, on one device; each keeps its own fields, reachable through
- * os_batch_scenario() with the single-handle calls (upload, download, fields).
+ * Batched and served scenarios: many independent tunnels of different sizes
+ * advanced together, one CUDA graph per step and one persistent kernel per
+ * phase that walks the rows or tiles of all members. No reference counterpart
+ * (the reference runs one grid). Each member advances exactly as a single
+ * handle with the same sweeps-per-pass would: the same per-cell and per-tile
+ * code runs, only the schedule differs. Members are FP32, FP16 or BF16 storage
+ * with pressure off, on the batch's device, with projection_n at most 128 x
+ * block_k; each keeps its own fields, reachable through os_batch_scenario()
+ * with the single-handle calls (upload, download, fields). Calls on one batch
+ * come from one thread.
+ *
+ * Membership can change between steps (continuous batching): os_batch_add
+ * admits a scenario for a number of steps, it joins at the next os_batch_step
+ * and stops on the device after exactly that many of the batch's steps;
+ * os_batch_poll reports finished members, whose fields stay readable until
+ * os_batch_remove. With a device-memory budget the batch reserves it once and
+ * places every member inside it, so os_batch_add says OS_ERR_NOMEM without
+ * touching the device when a scenario does not fit.
  */
 typedef struct os_batch os_batch;
 
 typedef struct os_batch_stats {
-  int32_t scenarios;
+  int32_t scenarios;          /* members, finished or not */
   int32_t block_k;            /* sweeps per blocked pass */
   int32_t kernels_per_step;   /* launches in one step's graph */
-  int32_t reserved;
-  int64_t cells;              /* total cells over all scenarios */
+  int32_t members_in_plan;    /* members the next step advances */
+  int64_t cells;              /* cells over the members in the plan */
   int64_t launches;           /* kernels launched by os_batch_step so far */
   int64_t tile_items_per_step;
+  int64_t steps_enqueued;     /* batch steps enqueued so far */
+  int64_t steps_completed;    /* of those, seen complete by the host */
 } os_batch_stats;
 
-/* `block_k`: sweeps per blocked pass for every scenario (0 = 8). */
+typedef enum os_member_state {
+  OS_MEMBER_WAITING = 0, /* admitted, joins at the next os_batch_step */
+  OS_MEMBER_RUNNING = 1,
+  OS_MEMBER_DONE = 2     /* all its steps have completed on the device */
+} os_member_state;
+
+/* A batch of fixed members, each stepping until the batch is destroyed; member
+ * ids are 0..count-1. `block_k`: sweeps per blocked pass (0 = 8, at most 16). */
 int os_batch_create(const os_config* cfgs, int32_t count, int32_t block_k, os_batch** out);
+/* An empty batch on `device` for continuous batching. `budget_bytes` > 0
+ * reserves that much device memory for the members (0: each member allocates
+ * its own, without a limit). */
+int os_batch_create_dynamic(int32_t device, int32_t block_k, uint64_t budget_bytes,
+                            os_batch** out);
+/* Admits a scenario for `steps` steps (negative: until removed); its id goes
+ * to *id. Its fields start as os_create leaves them and may be uploaded
+ * before the next os_batch_step. OS_ERR_NOMEM: it does not fit the budget. */
+int os_batch_add(os_batch* b, const os_config* cfg, int32_t steps, int64_t* id);
+/* Drops a member and returns its memory (a running member is cancelled; its
+ * memory is returned once the steps already enqueued have run). */
+int os_batch_remove(os_batch* b, int64_t id);
 int os_batch_destroy(os_batch* b);
-/* `steps` steps of every scenario (graph replays) enqueued on `stream` (NULL:
- * the batch's own stream); each scenario uses its own config's d_t. */
+/* `steps` steps of every member (graph replays) enqueued on `stream` (NULL:
+ * the batch's own stream); each member uses its own config's d_t. Membership
+ * changes since the last call take effect first, ordered on the same stream. */
 int os_batch_step(os_batch* b, int32_t steps, void* stream);
 int os_batch_synchronize(os_batch* b);
-/* The handle of scenario `index`, owned by the batch (do not destroy it). */
-int os_batch_scenario(os_batch* b, int32_t index, os_handle** out);
+/* Ids of members whose last step has completed and that were not reported
+ * before, at most `cap` of them; with `wait`, blocks until at least one
+ * finishes when one is due within the steps already enqueued. */
+int os_batch_poll(os_batch* b, int32_t wait, int64_t* ids, int32_t cap, int32_t* count);
+/* Blocks until at most `max_in_flight` enqueued steps have not completed
+ * (0: all of them), for pacing a loop that enqueues ahead. */
+int os_batch_wait(os_batch* b, int64_t max_in_flight);
+/* A member's state (os_member_state) and steps still to run (-1: unlimited). */
+int os_batch_status(os_batch* b, int64_t id, int32_t* state, int64_t* steps_left);
+/* Device bytes held by the members, and the budget (0: none). */
+int os_batch_memory(os_batch* b, uint64_t* used, uint64_t* budget);
+/* The handle of member `id`, owned by the batch (do not destroy it). */
+int os_batch_scenario(os_batch* b, int64_t id, os_handle** out);
 int os_batch_info(os_batch* b, os_batch_stats* out);
 
 #ifdef __cplusplus

@@ -267,14 +267,15 @@ __device__ __forceinline__ void proj_half_sweep(float* __restrict__ S,
 // p is staged for owned cells only (halo pressure is never needed), so no CTA
 // reads pressure that another CTA writes in the same pass.
 // One tile (tx, ty) of one grid: stage, `sweeps` red/black sweeps, write back.
+// The three parts are separate so that a caller holding several storage types
+// instantiates the sweeps once.
 template <bool PRESSURE, class S>
-__device__ __forceinline__ void project_tile(float* smem, int tx, int ty,
-                                             const S* __restrict__ u_in,
-                                             const S* __restrict__ v_in, S* __restrict__ u_out,
-                                             S* __restrict__ v_out, float* __restrict__ p,
-                                             const uint8_t* __restrict__ fl, const Consts& c,
-                                             const StepParams* __restrict__ prm, int sweeps,
-                                             int halo, int TX, int TY, int zero_pressure) {
+__device__ __forceinline__ void proj_stage_in(float* smem, int tx, int ty,
+                                              const S* __restrict__ u_in,
+                                              const S* __restrict__ v_in,
+                                              const float* __restrict__ p,
+                                              const uint8_t* __restrict__ fl, const Consts& c,
+                                              int halo, int TX, int TY, int zero_pressure) {
   const int RH = TY + 2 * halo;
   const ProjPlanes P = proj_planes<PRESSURE>(smem, RH);
   const int gx0 = tx * TX - halo, gy0 = ty * TY - halo;
@@ -319,7 +320,15 @@ __device__ __forceinline__ void project_tile(float* smem, int tx, int ty,
       ((x & 1) ? P.po : P.pe)[y * kHalfW + (x >> 1)] = pp;
     }
   }
-  __syncthreads();
+}
+
+// `sweeps` red/black sweeps on the staged tile; ends with a barrier.
+template <bool PRESSURE>
+__device__ __forceinline__ void proj_sweeps(float* smem, const Consts& c,
+                                            const StepParams* __restrict__ prm, int sweeps,
+                                            int halo, int TY) {
+  const int RH = TY + 2 * halo;
+  const ProjPlanes P = proj_planes<PRESSURE>(smem, RH);
   const float d_t = prm->dt;
   const int plane = RH * kHalfW + kArrPad;
   const int fo_off = RH * kHalfW + 64;
@@ -330,7 +339,18 @@ __device__ __forceinline__ void project_tile(float* smem, int tx, int ty,
     proj_half_sweep<1, PRESSURE>(smem, P.fe, plane, fo_off, RH, halo, reach - 1, c, d_t);
     __syncthreads();
   }
-  // Owned cells back out; halo and TX are multiples of 4 when `vec` holds.
+}
+
+// Owned cells back out; halo and TX are multiples of 4 when `vec` holds.
+template <bool PRESSURE, class S>
+__device__ __forceinline__ void proj_stage_out(float* smem, int tx, int ty, S* __restrict__ u_out,
+                                               S* __restrict__ v_out, float* __restrict__ p,
+                                               const Consts& c, int halo, int TX, int TY) {
+  const int RH = TY + 2 * halo;
+  const ProjPlanes P = proj_planes<PRESSURE>(smem, RH);
+  const int gx0 = tx * TX - halo, gy0 = ty * TY - halo;
+  const int W = c.W, H = c.H;
+  const bool vec = ((W & 3) == 0) && ((gx0 & 3) == 0);
   for (int it = threadIdx.x; it < TY * kQuads; it += blockDim.x) {
     const int y = halo + it / kQuads, x = 4 * (it % kQuads);
     const int i = gx0 + x, j = gy0 + y;
@@ -360,6 +380,20 @@ __device__ __forceinline__ void project_tile(float* smem, int tx, int ty,
       if (PRESSURE) p[gk] = (xd & 1) ? P.po[sd] : P.pe[sd];
     }
   }
+}
+
+template <bool PRESSURE, class S>
+__device__ __forceinline__ void project_tile(float* smem, int tx, int ty,
+                                             const S* __restrict__ u_in,
+                                             const S* __restrict__ v_in, S* __restrict__ u_out,
+                                             S* __restrict__ v_out, float* __restrict__ p,
+                                             const uint8_t* __restrict__ fl, const Consts& c,
+                                             const StepParams* __restrict__ prm, int sweeps,
+                                             int halo, int TX, int TY, int zero_pressure) {
+  proj_stage_in<PRESSURE, S>(smem, tx, ty, u_in, v_in, p, fl, c, halo, TX, TY, zero_pressure);
+  __syncthreads();
+  proj_sweeps<PRESSURE>(smem, c, prm, sweeps, halo, TY);
+  proj_stage_out<PRESSURE, S>(smem, tx, ty, u_out, v_out, p, c, halo, TX, TY);
 }
 
 template <bool PRESSURE, class S>

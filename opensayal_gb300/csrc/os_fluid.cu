@@ -21,6 +21,7 @@
 #include <mutex>
 #include <new>
 #include <tuple>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/opensayal_gb300.h"
@@ -57,6 +58,77 @@ size_t storage_bytes(int storage) {
   }
 }
 
+// Device memory with a byte budget: one cudaMalloc up front, carved into
+// 256-byte-aligned blocks, best fit, neighbouring free blocks merged on
+// release. Admission against the budget is then a host-side decision that
+// never touches the driver.
+class Arena {
+ public:
+  int init(size_t bytes) {
+    capacity_ = (bytes + kAlign - 1) / kAlign * kAlign;
+    cudaError_t e = cudaMalloc(&base_, capacity_);
+    if (e != cudaSuccess) {
+      base_ = nullptr;
+      return OS_ERR_NOMEM;
+    }
+    free_[0] = capacity_;
+    return OS_OK;
+  }
+  ~Arena() {
+    if (base_) cudaFree(base_);
+  }
+  void* alloc(size_t bytes) {
+    std::lock_guard<std::mutex> lock(mu_);
+    const size_t n = std::max<size_t>(kAlign, (bytes + kAlign - 1) / kAlign * kAlign);
+    auto best = free_.end();
+    for (auto it = free_.begin(); it != free_.end(); ++it)
+      if (it->second >= n && (best == free_.end() || it->second < best->second)) best = it;
+    if (best == free_.end()) return nullptr;
+    const size_t off = best->first, size = best->second;
+    free_.erase(best);
+    if (size > n) free_[off + n] = size - n;
+    live_[off] = n;
+    used_ += n;
+    return base_ + off;
+  }
+  void release(void* p) {
+    std::lock_guard<std::mutex> lock(mu_);
+    const size_t off = static_cast<char*>(p) - base_;
+    auto it = live_.find(off);
+    if (it == live_.end()) return;
+    size_t start = off, size = it->second;
+    used_ -= size;
+    live_.erase(it);
+    auto next = free_.lower_bound(start);
+    if (next != free_.end() && start + size == next->first) {
+      size += next->second;
+      next = free_.erase(next);
+    }
+    if (next != free_.begin()) {
+      auto prev = std::prev(next);
+      if (prev->first + prev->second == start) {
+        start = prev->first;
+        size += prev->second;
+        free_.erase(prev);
+      }
+    }
+    free_[start] = size;
+  }
+  bool owns(const void* p) const {
+    return base_ && p >= base_ && static_cast<const char*>(p) < base_ + capacity_;
+  }
+  size_t used() const { return used_; }
+  size_t capacity() const { return capacity_; }
+
+ private:
+  static constexpr size_t kAlign = 256;
+  char* base_ = nullptr;
+  size_t capacity_ = 0, used_ = 0;
+  std::map<size_t, size_t> free_;  // offset -> size
+  std::map<size_t, size_t> live_;  // offset -> size
+  std::mutex mu_;
+};
+
 }  // namespace
 
 struct os_handle {
@@ -88,7 +160,46 @@ struct os_handle {
   int kernels_per_step = 0;
   int64_t launches = 0;
   float min_pressure = 0.0f, max_pressure = 0.0f;
+  // Device memory: one arena block carved in order, or one cudaMalloc each.
+  Arena* arena = nullptr;
+  char* arena_block = nullptr;
+  size_t arena_size = 0, arena_used = 0;
+  size_t device_bytes = 0;  // device memory this handle holds
 };
+
+namespace {
+
+// Device bytes a handle of this configuration takes from an arena: fields and
+// their buffers, pressure, mask, counts, flags, the parameter block, the
+// pressure keys and, for 16-bit storage, the FP32 transfer staging.
+size_t handle_footprint(const os_config& c) {
+  const size_t N = (size_t)c.width * c.height;
+  const size_t e = storage_bytes(c.storage);
+  auto r = [](size_t b) { return (b + 255) / 256 * 256; };
+  size_t bytes = 6 * r(N * e) + 3 * r(N * 4) + r(N) + r(sizeof(StepParams)) + r(2 * sizeof(int));
+  if (c.storage != OS_STORAGE_F32) bytes += r(N * 4);
+  return bytes;
+}
+
+cudaError_t dev_alloc(os_handle* h, void** p, size_t bytes) {
+  if (h->arena_block) {
+    const size_t off = (h->arena_used + 255) / 256 * 256;
+    if (off + bytes > h->arena_size) return cudaErrorMemoryAllocation;
+    *p = h->arena_block + off;
+    h->arena_used = off + bytes;
+  } else {
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) return e;
+    h->device_bytes += bytes;
+  }
+  return cudaSuccess;
+}
+
+void dev_free(os_handle* h, void* p) {
+  if (p && !h->arena_block) cudaFree(p);
+}
+
+}  // namespace
 
 // The temporally blocked projection/diffusion engine works on the handle.
 #include "os_blocked.cuh"
@@ -363,12 +474,18 @@ int push_params(os_handle* h, const os_source* src, float dt, cudaStream_t st) {
     p.src_y = src->position_y;
   }
   if (h->params_valid && memcmp(&p, &h->last_params, sizeof p) == 0) return OS_OK;
-  // Pinned staging slot; the previous copy out of it must have completed
-  // before it is rewritten.
-  CUDA_OR_RETURN(cudaEventSynchronize(h->params_event));
-  *h->h_params = p;
-  CUDA_OR_RETURN(cudaMemcpyAsync(h->d_params, h->h_params, sizeof p, cudaMemcpyHostToDevice, st));
-  CUDA_OR_RETURN(cudaEventRecord(h->params_event, st));
+  if (h->h_params) {
+    // Pinned staging slot; the previous copy out of it must have completed
+    // before it is rewritten.
+    CUDA_OR_RETURN(cudaEventSynchronize(h->params_event));
+    *h->h_params = p;
+    CUDA_OR_RETURN(cudaMemcpyAsync(h->d_params, h->h_params, sizeof p, cudaMemcpyHostToDevice, st));
+    CUDA_OR_RETURN(cudaEventRecord(h->params_event, st));
+  } else {
+    // Handles without a pinned slot (scenarios of a batch): a pageable copy,
+    // staged by the driver before the call returns.
+    CUDA_OR_RETURN(cudaMemcpyAsync(h->d_params, &p, sizeof p, cudaMemcpyHostToDevice, st));
+  }
   h->params_bytes += sizeof p;
   h->last_params = p;
   h->params_valid = true;
@@ -404,8 +521,8 @@ void free_handle(os_handle* h) {
   if (h->graph) cudaGraphExecDestroy(h->graph);
   void* ptrs[] = {h->u, h->v, h->s, h->ub, h->vb, h->sb, h->p, h->is_solid,
                   h->total_s, h->flags, h->d_params, h->d_pkeys, h->conv};
-  for (void* q : ptrs)
-    if (q) cudaFree(q);
+  for (void* q : ptrs) dev_free(h, q);
+  if (h->arena_block) h->arena->release(h->arena_block);
   if (h->h_pkeys) cudaFreeHost(h->h_pkeys);
   if (h->h_params) cudaFreeHost(h->h_params);
   if (h->params_event) cudaEventDestroy(h->params_event);
@@ -522,11 +639,11 @@ int os_config_defaults(int32_t width, int32_t height, os_config* out) {
   return OS_OK;
 }
 
-int os_create(const os_config* cfg, os_handle** out) {
-  if (!cfg || !out) return set_err(OS_ERR_INVALID, "null argument");
-  *out = nullptr;
-  int rc = validate(cfg);
-  if (rc) return rc;
+// A validated configuration becomes a handle. With an arena, the device
+// memory is one block of it (carved by dev_alloc) and the handle gets no
+// pinned host slots: such handles are the scenarios of a batch, whose
+// creation and release must not stall the device.
+static int create_handle(const os_config* cfg, Arena* arena, os_handle** out) {
   os_handle* h = new (std::nothrow) os_handle();
   if (!h) return set_err(OS_ERR_NOMEM, "host allocation failed");
   h->cfg = *cfg;
@@ -569,27 +686,38 @@ int os_create(const os_config* cfg, os_handle** out) {
   cudaError_t e = cudaSetDevice(cfg->device);
   if (e != cudaSuccess)
     return fail(set_err(OS_ERR_CUDA, "cudaSetDevice(%d): %s", cfg->device, cudaGetErrorString(e)));
+  if (arena) {
+    h->arena = arena;
+    h->arena_size = handle_footprint(*cfg);
+    h->arena_block = static_cast<char*>(arena->alloc(h->arena_size));
+    if (!h->arena_block)
+      return fail(set_err(OS_ERR_NOMEM, "device budget: %zu bytes needed, %zu of %zu in use",
+                          h->arena_size, arena->used(), arena->capacity()));
+    h->device_bytes = h->arena_size;
+  }
   if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess)
     return fail(set_err(OS_ERR_CUDA, "stream: %s", cudaGetErrorString(e)));
   const size_t fb = h->N * h->esize;
   void** fields[] = {&h->u, &h->v, &h->s, &h->ub, &h->vb, &h->sb};
   for (void** f : fields) {
-    if ((e = cudaMalloc(f, fb)) != cudaSuccess)
+    if ((e = dev_alloc(h, f, fb)) != cudaSuccess)
       return fail(set_err(OS_ERR_NOMEM, "cudaMalloc(%zu): %s", fb, cudaGetErrorString(e)));
     cudaMemsetAsync(*f, 0, fb, h->stream);
   }
-  if ((e = cudaMalloc(&h->p, h->N * 4)) != cudaSuccess ||
-      (e = cudaMalloc(&h->is_solid, h->N * 4)) != cudaSuccess ||
-      (e = cudaMalloc(&h->total_s, h->N * 4)) != cudaSuccess ||
-      (e = cudaMalloc(&h->flags, h->N)) != cudaSuccess ||
-      (e = cudaMalloc(&h->d_params, sizeof(StepParams))) != cudaSuccess ||
-      (e = cudaMalloc(&h->d_pkeys, 2 * sizeof(int))) != cudaSuccess)
+  if ((e = dev_alloc(h, (void**)&h->p, h->N * 4)) != cudaSuccess ||
+      (e = dev_alloc(h, (void**)&h->is_solid, h->N * 4)) != cudaSuccess ||
+      (e = dev_alloc(h, (void**)&h->total_s, h->N * 4)) != cudaSuccess ||
+      (e = dev_alloc(h, (void**)&h->flags, h->N)) != cudaSuccess ||
+      (e = dev_alloc(h, (void**)&h->d_params, sizeof(StepParams))) != cudaSuccess ||
+      (e = dev_alloc(h, (void**)&h->d_pkeys, 2 * sizeof(int))) != cudaSuccess)
     return fail(set_err(OS_ERR_NOMEM, "cudaMalloc: %s", cudaGetErrorString(e)));
-  if ((e = cudaMallocHost(&h->h_pkeys, 2 * sizeof(int))) != cudaSuccess ||
-      (e = cudaMallocHost(&h->h_params, sizeof(StepParams))) != cudaSuccess)
-    return fail(set_err(OS_ERR_NOMEM, "cudaMallocHost: %s", cudaGetErrorString(e)));
-  if ((e = cudaEventCreateWithFlags(&h->params_event, cudaEventDisableTiming)) != cudaSuccess)
-    return fail(set_err(OS_ERR_CUDA, "event: %s", cudaGetErrorString(e)));
+  if (!arena) {
+    if ((e = cudaMallocHost(&h->h_pkeys, 2 * sizeof(int))) != cudaSuccess ||
+        (e = cudaMallocHost(&h->h_params, sizeof(StepParams))) != cudaSuccess)
+      return fail(set_err(OS_ERR_NOMEM, "cudaMallocHost: %s", cudaGetErrorString(e)));
+    if ((e = cudaEventCreateWithFlags(&h->params_event, cudaEventDisableTiming)) != cudaSuccess)
+      return fail(set_err(OS_ERR_CUDA, "event: %s", cudaGetErrorString(e)));
+  }
   cudaMemsetAsync(h->p, 0, h->N * 4, h->stream);
   MaskParams m;
   m.enable_drain = cfg->enable_drain != 0;
@@ -610,6 +738,14 @@ int os_create(const os_config* cfg, os_handle** out) {
     h->block_k = h->storage != OS_STORAGE_F64 ? autotune_block_k(*cfg) : -1;
   *out = h;
   return OS_OK;
+}
+
+int os_create(const os_config* cfg, os_handle** out) {
+  if (!cfg || !out) return set_err(OS_ERR_INVALID, "null argument");
+  *out = nullptr;
+  int rc = validate(cfg);
+  if (rc) return rc;
+  return create_handle(cfg, nullptr, out);
 }
 
 int os_destroy(os_handle* h) {
@@ -695,7 +831,7 @@ int os_upload(os_handle* h, int32_t field, const void* host, size_t count) {
   if (!storage_field || h->storage == OS_STORAGE_F32) {
     CUDA_OR_RETURN(cudaMemcpyAsync(dst, host, h->N * 4, cudaMemcpyHostToDevice, h->stream));
   } else {
-    if (!h->conv) CUDA_OR_RETURN(cudaMalloc(&h->conv, h->N * 4));
+    if (!h->conv) CUDA_OR_RETURN(dev_alloc(h, (void**)&h->conv, h->N * 4));
     CUDA_OR_RETURN(cudaMemcpyAsync(h->conv, host, h->N * 4, cudaMemcpyHostToDevice, h->stream));
     if ((rc = convert(h, dst, true))) return rc;
   }
@@ -714,7 +850,7 @@ int os_download(os_handle* h, int32_t field, void* host, size_t count) {
   if (!storage_field || h->storage == OS_STORAGE_F32) {
     CUDA_OR_RETURN(cudaMemcpyAsync(host, src, h->N * 4, cudaMemcpyDeviceToHost, h->stream));
   } else {
-    if (!h->conv) CUDA_OR_RETURN(cudaMalloc(&h->conv, h->N * 4));
+    if (!h->conv) CUDA_OR_RETURN(dev_alloc(h, (void**)&h->conv, h->N * 4));
     if ((rc = convert(h, src, false))) return rc;
     CUDA_OR_RETURN(cudaMemcpyAsync(host, h->conv, h->N * 4, cudaMemcpyDeviceToHost, h->stream));
   }
@@ -967,253 +1103,5 @@ extern "C" int os_diffuse_noalloc(const os_config* cfg, float* u, float dt, void
   return OS_OK;
 }
 
-// ===========================================================================
-// Batched scenarios (os_batch_*)
-// ===========================================================================
-
-#include "os_batch.cuh"
-
-struct os_batch {
-  std::vector<os_handle*> handles;
-  int K = 8;
-  int device = 0;
-  int sms = 152;
-  cudaStream_t stream = nullptr;
-  ScenarioDesc* d_table = nullptr;
-  RowItem* d_rows = nullptr;
-  TileItem* d_tiles = nullptr;
-  int n_rows = 0;
-  std::vector<int> diff_off, diff_cnt, proj_off, proj_cnt;
-  TileGeom gd{}, gp{};
-  cudaGraphExec_t graph = nullptr;
-  int kernels_per_step = 0;
-  int64_t launches = 0;
-  int64_t cells = 0;
-};
-
-namespace {
-
-// Largest even tile height whose region fits shared memory.
-TileGeom batch_geom(int halo, bool projection) {
-  TileGeom g{};
-  g.halo = halo;
-  g.TX = kRegionW - 2 * halo;
-  int TY = 2;
-  while (true) {
-    const int next = TY + 2;
-    const size_t sm = projection ? projection_smem(next + 2 * halo, false)
-                                 : diffusion_smem(next + 2 * halo);
-    if (sm > kMaxSmem) break;
-    TY = next;
-  }
-  g.TY = TY;
-  g.RH = TY + 2 * halo;
-  g.smem = projection ? projection_smem(g.RH, false) : diffusion_smem(g.RH);
-  return g;
-}
-
-void free_batch(os_batch* b) {
-  if (!b) return;
-  if (b->graph) cudaGraphExecDestroy(b->graph);
-  if (b->d_table) cudaFree(b->d_table);
-  if (b->d_rows) cudaFree(b->d_rows);
-  if (b->d_tiles) cudaFree(b->d_tiles);
-  if (b->stream) cudaStreamDestroy(b->stream);
-  for (os_handle* h : b->handles) os_destroy(h);
-  delete b;
-}
-
-int build_batch_graph(os_batch* b) {
-  cudaStream_t st = b->stream;
-  const int count = (int)b->handles.size();
-  int kernels = 0;
-  CUDA_OR_RETURN(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-  const int row_grid = std::min(b->n_rows, b->sms * 16);
-  k_batch_forces<<<row_grid, 128, 0, st>>>(b->d_rows, b->n_rows, b->d_table);
-  kernels++;
-  for (size_t p = 0; p < b->diff_cnt.size(); p++) {
-    const int cnt = b->diff_cnt[p];
-    k_batch_diffuse<<<std::min(cnt, b->sms), kBlockThreads, b->gd.smem, st>>>(
-        b->d_tiles + b->diff_off[p], cnt, b->d_table, (int)p, b->K, b->gd.halo, b->gd.TX,
-        b->gd.TY);
-    kernels++;
-  }
-  for (size_t p = 0; p < b->proj_cnt.size(); p++) {
-    const int cnt = b->proj_cnt[p];
-    k_batch_project<<<std::min(cnt, b->sms), kBlockThreads, b->gp.smem, st>>>(
-        b->d_tiles + b->proj_off[p], cnt, b->d_table, (int)p, b->K, b->gp.halo, b->gp.TX,
-        b->gp.TY);
-    kernels++;
-  }
-  k_batch_extrapolate<<<std::min(count, b->sms * 4), 1024, 0, st>>>(b->d_table, count);
-  k_batch_advect_velocity<<<row_grid, 128, 0, st>>>(b->d_rows, b->n_rows, b->d_table);
-  k_batch_advect_smoke<<<row_grid, 128, 0, st>>>(b->d_rows, b->n_rows, b->d_table);
-  k_batch_finish_smoke<<<row_grid, 128, 0, st>>>(b->d_rows, b->n_rows, b->d_table);
-  kernels += 4;
-  const cudaError_t le = cudaGetLastError();
-  cudaGraph_t g = nullptr;
-  const cudaError_t ce = cudaStreamEndCapture(st, &g);
-  if (le != cudaSuccess) {
-    if (g) cudaGraphDestroy(g);
-    return set_err(OS_ERR_CUDA, "batch launch: %s", cudaGetErrorString(le));
-  }
-  if (ce != cudaSuccess) return set_err(OS_ERR_CUDA, "batch capture: %s", cudaGetErrorString(ce));
-  const cudaError_t ie = cudaGraphInstantiate(&b->graph, g, 0);
-  cudaGraphDestroy(g);
-  if (ie != cudaSuccess) return set_err(OS_ERR_CUDA, "batch instantiate: %s", cudaGetErrorString(ie));
-  b->kernels_per_step = kernels;
-  return OS_OK;
-}
-
-}  // namespace
-
-extern "C" {
-
-int os_batch_create(const os_config* cfgs, int32_t count, int32_t block_k, os_batch** out) {
-  if (!cfgs || !out || count < 1) return set_err(OS_ERR_INVALID, "bad argument");
-  *out = nullptr;
-  const int K = block_k > 0 ? std::min(block_k, 16) : 8;
-  for (int i = 0; i < count; i++) {
-    const os_config& c = cfgs[i];
-    int rc = validate(&c);
-    if (rc) return rc;
-    if (c.storage != OS_STORAGE_F32 || c.enable_pressure || c.device != cfgs[0].device)
-      return set_err(OS_ERR_UNSUPPORTED,
-                     "batched scenarios are FP32, pressure off, on one device (scenario %d)", i);
-  }
-  os_batch* b = new (std::nothrow) os_batch();
-  if (!b) return set_err(OS_ERR_NOMEM, "host allocation failed");
-  b->K = K;
-  b->device = cfgs[0].device;
-  b->sms = sm_count(b->device);
-  auto fail = [&](int code) {
-    free_batch(b);
-    return code;
-  };
-  cudaError_t e = cudaSetDevice(b->device);
-  if (e != cudaSuccess) return fail(set_err(OS_ERR_CUDA, "cudaSetDevice: %s", cudaGetErrorString(e)));
-  if ((e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking)) != cudaSuccess)
-    return fail(set_err(OS_ERR_CUDA, "stream: %s", cudaGetErrorString(e)));
-  b->gd = batch_geom(K, false);
-  b->gp = batch_geom(2 * K, true);
-  std::vector<ScenarioDesc> table;
-  std::vector<RowItem> rows;
-  for (int i = 0; i < count; i++) {
-    os_config c = cfgs[i];
-    c.projection_block = K;
-    os_handle* h = nullptr;
-    int rc = os_create(&c, &h);
-    if (rc) return fail(rc);
-    b->handles.push_back(h);
-    if ((rc = push_params(h, nullptr, c.d_t, h->stream))) return fail(rc);
-    ScenarioDesc d{};
-    d.c = h->c;
-    d.smoke_period = h->smoke_period;
-    d.smoke_on = c.enable_smoke && c.tunnel_smoke != 0.0f;
-    d.proj_passes = (h->c.n + K - 1) / K;
-    d.diff_passes = c.viscosity != 0.0f ? d.proj_passes : 0;
-    d.prm = h->d_params;
-    d.u = static_cast<float*>(h->u);
-    d.v = static_cast<float*>(h->v);
-    d.ub = static_cast<float*>(h->ub);
-    d.vb = static_cast<float*>(h->vb);
-    d.s = static_cast<float*>(h->s);
-    d.sb = static_cast<float*>(h->sb);
-    d.flags = h->flags;
-    table.push_back(d);
-    for (int j = 0; j < h->H; j++) rows.push_back(RowItem{i, j});
-    b->cells += (int64_t)h->N;
-  }
-  // Tile lists: pass p of a phase lists the tiles of every scenario that
-  // still has a pass p to do.
-  std::vector<TileItem> tiles;
-  auto add_passes = [&](const TileGeom& g, bool diffusion, std::vector<int>& off,
-                        std::vector<int>& cnt) {
-    int max_passes = 0;
-    for (const ScenarioDesc& d : table)
-      max_passes = std::max(max_passes, diffusion ? d.diff_passes : d.proj_passes);
-    for (int p = 0; p < max_passes; p++) {
-      off.push_back((int)tiles.size());
-      for (int s = 0; s < count; s++) {
-        const ScenarioDesc& d = table[s];
-        if ((diffusion ? d.diff_passes : d.proj_passes) <= p) continue;
-        const int tx_n = (d.c.W + g.TX - 1) / g.TX, ty_n = (d.c.H + g.TY - 1) / g.TY;
-        for (int ty = 0; ty < ty_n; ty++)
-          for (int tx = 0; tx < tx_n; tx++) tiles.push_back(TileItem{s, tx, ty});
-      }
-      cnt.push_back((int)tiles.size() - off.back());
-    }
-  };
-  add_passes(b->gd, true, b->diff_off, b->diff_cnt);
-  add_passes(b->gp, false, b->proj_off, b->proj_cnt);
-  b->n_rows = (int)rows.size();
-  if ((e = cudaMalloc(&b->d_table, table.size() * sizeof(ScenarioDesc))) != cudaSuccess ||
-      (e = cudaMalloc(&b->d_rows, rows.size() * sizeof(RowItem))) != cudaSuccess ||
-      (e = cudaMalloc(&b->d_tiles, std::max<size_t>(1, tiles.size()) * sizeof(TileItem))) !=
-          cudaSuccess)
-    return fail(set_err(OS_ERR_NOMEM, "batch tables: %s", cudaGetErrorString(e)));
-  cudaMemcpy(b->d_table, table.data(), table.size() * sizeof(ScenarioDesc), cudaMemcpyHostToDevice);
-  cudaMemcpy(b->d_rows, rows.data(), rows.size() * sizeof(RowItem), cudaMemcpyHostToDevice);
-  if (!tiles.empty())
-    cudaMemcpy(b->d_tiles, tiles.data(), tiles.size() * sizeof(TileItem), cudaMemcpyHostToDevice);
-  for (os_handle* h : b->handles) cudaStreamSynchronize(h->stream);
-  cudaFuncSetAttribute(k_batch_diffuse, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)b->gd.smem);
-  cudaFuncSetAttribute(k_batch_project, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)b->gp.smem);
-  if ((e = cudaDeviceSynchronize()) != cudaSuccess)
-    return fail(set_err(OS_ERR_CUDA, "batch set-up: %s", cudaGetErrorString(e)));
-  int rc = build_batch_graph(b);
-  if (rc) return fail(rc);
-  *out = b;
-  return OS_OK;
-}
-
-int os_batch_destroy(os_batch* b) {
-  if (!b) return OS_OK;
-  cudaSetDevice(b->device);
-  cudaStreamSynchronize(b->stream);
-  free_batch(b);
-  return OS_OK;
-}
-
-int os_batch_step(os_batch* b, int32_t steps, void* stream) {
-  if (!b || steps < 0) return set_err(OS_ERR_INVALID, "bad argument");
-  int cur = -1;
-  CUDA_OR_RETURN(cudaGetDevice(&cur));
-  if (cur != b->device) CUDA_OR_RETURN(cudaSetDevice(b->device));
-  cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : b->stream;
-  for (int t = 0; t < steps; t++) CUDA_OR_RETURN(cudaGraphLaunch(b->graph, st));
-  b->launches += (int64_t)steps * b->kernels_per_step;
-  return OS_OK;
-}
-
-int os_batch_synchronize(os_batch* b) {
-  if (!b) return set_err(OS_ERR_INVALID, "null batch");
-  CUDA_OR_RETURN(cudaStreamSynchronize(b->stream));
-  return OS_OK;
-}
-
-int os_batch_scenario(os_batch* b, int32_t index, os_handle** out) {
-  if (!b || !out || index < 0 || index >= (int)b->handles.size())
-    return set_err(OS_ERR_INVALID, "bad scenario index");
-  *out = b->handles[index];
-  return OS_OK;
-}
-
-int os_batch_info(os_batch* b, os_batch_stats* out) {
-  if (!b || !out) return set_err(OS_ERR_INVALID, "null argument");
-  memset(out, 0, sizeof *out);
-  out->scenarios = (int32_t)b->handles.size();
-  out->block_k = b->K;
-  out->kernels_per_step = b->kernels_per_step;
-  out->cells = b->cells;
-  out->launches = b->launches;
-  int64_t tiles = 0;
-  for (int c : b->diff_cnt) tiles += c;
-  for (int c : b->proj_cnt) tiles += c;
-  out->tile_items_per_step = tiles;
-  return OS_OK;
-}
-
-}  // extern "C"
+// Batched and served scenarios: os_batch_*, built on the handles above.
+#include "os_batch_host.cuh"

@@ -126,10 +126,21 @@ SIGNATURES = [
     ("os_diffuse_noalloc", C.c_int, [C.POINTER(OsConfig), C.c_void_p, C.c_float, C.c_void_p]),
     ("os_batch_create", C.c_int, [C.POINTER(OsConfig), C.c_int32, C.c_int32,
                                   C.POINTER(C.c_void_p)]),
+    ("os_batch_create_dynamic", C.c_int, [C.c_int32, C.c_int32, C.c_uint64,
+                                          C.POINTER(C.c_void_p)]),
+    ("os_batch_add", C.c_int, [C.c_void_p, C.POINTER(OsConfig), C.c_int32,
+                               C.POINTER(C.c_int64)]),
+    ("os_batch_remove", C.c_int, [C.c_void_p, C.c_int64]),
     ("os_batch_destroy", C.c_int, [C.c_void_p]),
     ("os_batch_step", C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
     ("os_batch_synchronize", C.c_int, [C.c_void_p]),
-    ("os_batch_scenario", C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p)]),
+    ("os_batch_poll", C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int64), C.c_int32,
+                                C.POINTER(C.c_int32)]),
+    ("os_batch_wait", C.c_int, [C.c_void_p, C.c_int64]),
+    ("os_batch_status", C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_int32),
+                                  C.POINTER(C.c_int64)]),
+    ("os_batch_memory", C.c_int, [C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+    ("os_batch_scenario", C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_void_p)]),
     ("os_batch_info", C.c_int, [C.c_void_p, C.c_void_p]),
 ]
 
@@ -139,11 +150,16 @@ class OsBatchStats(C.Structure):
         ("scenarios", C.c_int32),
         ("block_k", C.c_int32),
         ("kernels_per_step", C.c_int32),
-        ("reserved", C.c_int32),
+        ("members_in_plan", C.c_int32),
         ("cells", C.c_int64),
         ("launches", C.c_int64),
         ("tile_items_per_step", C.c_int64),
+        ("steps_enqueued", C.c_int64),
+        ("steps_completed", C.c_int64),
     ]
+
+
+MEMBER_WAITING, MEMBER_RUNNING, MEMBER_DONE = 0, 1, 2
 
 _lib = None
 

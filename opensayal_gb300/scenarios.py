@@ -99,26 +99,62 @@ CONFIGS = {
 }
 
 
+def _draw_scenario(rng: np.random.Generator) -> OsConfig:
+    sizes = np.arange(128, 1025, 32)
+    w = int(rng.choice(sizes))
+    h = int(rng.choice(sizes))
+    c = default_config(w, h)
+    c.pipe_height = h // 4
+    c.tunnel_speed = float(rng.uniform(0.5, 3.0))
+    c.tunnel_smoke = 1.0
+    c.obstacle_center_x = int(rng.integers(w // 4, 3 * w // 4 + 1))
+    c.obstacle_center_y = int(rng.integers(h // 4, 3 * h // 4 + 1))
+    c.obstacle_radius = float(rng.uniform(4.0, 0.1 * h))
+    c.g = float(rng.uniform(-10.0, 0.0))
+    c.projection_n = int(rng.choice([50, 100, 200]))
+    c.projection_o = 1.9
+    c.d_t = 0.05
+    return c
+
+
 def batched_scenarios(count: int = 512, seed: int = 4) -> list[OsConfig]:
     """Uneven grids: W, H uniform in {128, 160, ..., 1024}, pipe H/4, inflow
     U[0.5, 3], obstacle centre integer-uniform over the middle half, radius
     U[4, 0.1 H], g U[-10, 0], n in {50, 100, 200}, o 1.9, dt 0.05."""
     rng = np.random.default_rng(seed)
-    sizes = np.arange(128, 1025, 32)
+    return [_draw_scenario(rng) for _ in range(count)]
+
+
+class Request:
+    """One served scenario: arrival time (s), config, step count and the seed
+    of its initial velocity perturbation."""
+
+    __slots__ = ("index", "arrival", "config", "steps", "seed")
+
+    def __init__(self, index, arrival, config, steps, seed):
+        self.index, self.arrival, self.config, self.steps, self.seed = (
+            index, arrival, config, steps, seed)
+
+    @property
+    def cells(self) -> int:
+        return self.config.width * self.config.height
+
+
+def serving_requests(rate: float = 200.0, seconds: float = 60.0, seed: int = 5,
+                     mixed_share: float = 0.5) -> list[Request]:
+    """Poisson arrivals at `rate` per second for `seconds`; each request is a
+    scenario drawn as in batched_scenarios with a step count uniform in
+    [100, 5000] and, with probability `mixed_share`, BF16 storage of u, v and
+    smoke (FP32 otherwise)."""
+    rng = np.random.default_rng(seed)
     out = []
-    for _ in range(count):
-        w = int(rng.choice(sizes))
-        h = int(rng.choice(sizes))
-        c = default_config(w, h)
-        c.pipe_height = h // 4
-        c.tunnel_speed = float(rng.uniform(0.5, 3.0))
-        c.tunnel_smoke = 1.0
-        c.obstacle_center_x = int(rng.integers(w // 4, 3 * w // 4 + 1))
-        c.obstacle_center_y = int(rng.integers(h // 4, 3 * h // 4 + 1))
-        c.obstacle_radius = float(rng.uniform(4.0, 0.1 * h))
-        c.g = float(rng.uniform(-10.0, 0.0))
-        c.projection_n = int(rng.choice([50, 100, 200]))
-        c.projection_o = 1.9
-        c.d_t = 0.05
-        out.append(c)
-    return out
+    t = 0.0
+    while True:
+        t += float(rng.exponential(1.0 / rate))
+        if t >= seconds:
+            return out
+        c = _draw_scenario(rng)
+        steps = int(rng.integers(100, 5001))
+        if rng.random() < mixed_share:
+            c.storage = 2  # OS_STORAGE_BF16
+        out.append(Request(len(out), t, c, steps, seed * 1_000_003 + len(out)))
