@@ -440,6 +440,69 @@ def run_serving(args, world, rank, local) -> dict | None:
     return res if rank == 0 else None
 
 
+def run_precision(args, world, rank, local) -> dict | None:
+    """Storage precision against an FP64 run of the same scheme: the 4096x4096
+    tunnel (n = 200, dt = 0.02) from the same seeded state, `--steps` steps in
+    FP32, FP16 and BF16 storage (FP32 arithmetic) and in FP64 storage and
+    arithmetic; per-field relative L2 against FP64 and the FP64 diagnostics of
+    every run. The workload can be scaled down with --precision-size."""
+    import torch
+    from opensayal_gb300 import Fluid, scenarios
+    from opensayal_gb300.build import build_library
+    build_library()
+    torch.cuda.set_device(local)
+    base = scenarios.large_config()
+    if args.precision_size:
+        s = args.precision_size / base.width
+        base.width = base.height = args.precision_size
+        base.pipe_height = int(base.pipe_height * s)
+        base.obstacle_center_x = base.obstacle_center_y = args.precision_size // 2
+        base.obstacle_radius = base.obstacle_radius * s
+        base.smoke_height = base.height // 4
+    base.device = local
+    steps = args.steps
+    fields = ("vel_x", "vel_y", "smoke")
+    runs = {}
+    for name, storage in (("f64", 3), ("f32", 0), ("f16", 1), ("bf16", 2)):
+        cfg = base.copy()
+        cfg.storage = storage
+        f = Fluid(cfg)
+        u, v = scenarios.perturbation(3, f.download("is_solid"))
+        f.upload("vel_x", u)
+        f.upload("vel_y", v)
+        t0 = time.perf_counter()
+        f.update_async(None, cfg.d_t, steps)
+        f.synchronize()
+        elapsed = time.perf_counter() - t0
+        runs[name] = {"fields": {k: f.download(k).astype(np.float64) for k in fields},
+                      "diag": f.diagnose(), "ms_per_step": elapsed * 1e3 / steps,
+                      "projection_block": f.fields().projection_block}
+        f.close()
+    ref = runs["f64"]
+    out = {}
+    for name, r in runs.items():
+        rel = {}
+        for k in fields:
+            den = float(np.linalg.norm(ref["fields"][k])) or 1.0
+            rel[k] = float(np.linalg.norm(r["fields"][k] - ref["fields"][k])) / den
+        dr = {}
+        for k in ("divergence_l2", "smoke_mass", "inflow_flux", "outflow_flux"):
+            den = abs(ref["diag"][k]) or 1.0
+            dr[k] = abs(r["diag"][k] - ref["diag"][k]) / den
+        out[name] = {"rel_l2_vs_f64": rel, "diag": r["diag"], "diag_rel_err_vs_f64": dr,
+                     "ms_per_step": r["ms_per_step"], "projection_block": r["projection_block"]}
+    cells = base.width * base.height
+    res = {
+        "metric": "relative L2 vs FP64 run of the same scheme", "value": out["bf16"]["rel_l2_vs_f64"]["vel_x"],
+        "unit": "relative L2 (u, bf16 storage)", "n_gpus": world, "steps": steps, "warmup": 0,
+        "ms_per_step": out["f32"]["ms_per_step"], "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32/f16/bf16 vs f64", "data": "synthetic",
+        "config": config_record(base, "precision", {"cells": cells}),
+        "variants": out,
+    }
+    return res if rank == 0 else None
+
+
 def run_reference(args, world, rank, local) -> dict | None:
     if rank != 0:
         return None
@@ -513,7 +576,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="default",
-                    choices=["default", "small", "large", "batched", "serving"])
+                    choices=["default", "small", "large", "batched", "serving", "precision"])
     ap.add_argument("--scenarios", type=int, default=512, help="batched workload size")
     ap.add_argument("--block", type=int, default=None,
                     help="red/black sweeps per blocked pass (0 autotune, -1 plain)")
@@ -527,6 +590,8 @@ def main():
     ap.add_argument("--serve-slots", type=int, default=64)
     ap.add_argument("--serve-chunk", type=int, default=2)
     ap.add_argument("--no-serial", action="store_true")
+    ap.add_argument("--precision-size", type=int, default=0,
+                    help="precision: square grid size instead of 4096")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -534,7 +599,8 @@ def main():
     if args.impl == "reference":
         res = run_reference(args, world, rank, local)
     else:
-        runner = {"batched": run_batched, "serving": run_serving}.get(args.workload, run_gb300)
+        runner = {"batched": run_batched, "serving": run_serving,
+                  "precision": run_precision}.get(args.workload, run_gb300)
         res = runner(args, world, rank, local)
     if res is not None:
         print(json.dumps(res), flush=True)

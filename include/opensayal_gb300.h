@@ -256,6 +256,28 @@ int os_profile_phase(os_handle* h, int32_t phase, const os_source* src, float dt
 int os_diffuse_noalloc(const os_config* cfg, float* u, float dt, void* stream);
 
 /*
+ * FP64 diagnostics of the current fields (no reference counterpart). The
+ * residual of a cell is the projection's divergence
+ * ((u(i+1,j) - u(i,j)) + v(i,j+1)) - v(i,j) (src/fluid.cu:229-262), taken in
+ * FP64 over the cells the projection updates; the sums are FP64 as well and
+ * are reduced in a fixed order, so repeated calls on the same fields agree bit
+ * for bit. Enqueued on the handle's stream after the work already there, and
+ * waits for the result.
+ */
+typedef struct os_diag {
+  double divergence_l2;   /* square root of the sum of squared residuals */
+  double divergence_max;  /* largest |residual| */
+  double divergence_sum;  /* sum of residuals */
+  double smoke_mass;      /* sum of smoke over fluid cells, times cell_size^2 */
+  double inflow_flux;     /* sum of u(2, j) between fluid cells (1, j), (2, j), times cell_size */
+  double outflow_flux;    /* sum of u(W-1, j) between fluid cells, times cell_size */
+  int64_t active_cells;   /* cells the projection updates */
+  int64_t reserved;
+} os_diag;
+
+int os_diagnose(os_handle* h, os_diag* out);
+
+/*
  * Batched and served scenarios: many independent tunnels of different sizes
  * advanced together, one CUDA graph per step and one persistent kernel per
  * phase that walks the rows or tiles of all members. No reference counterpart

@@ -156,6 +156,7 @@ struct os_handle {
   int* d_pkeys = nullptr;   // pressure extrema as ordered integer keys
   int* h_pkeys = nullptr;   // pinned copy
   float* conv = nullptr;    // FP32 staging for non-FP32 storage transfers
+  double* diag = nullptr;   // diagnostics partials and result (first use)
   cudaGraphExec_t graph = nullptr;
   int kernels_per_step = 0;
   int64_t launches = 0;
@@ -169,6 +170,9 @@ struct os_handle {
 
 namespace {
 
+// Diagnostics scratch: 256 block partials and the result, 7 doubles each.
+constexpr size_t kDiagBytes = (256 + 1) * 7 * sizeof(double);
+
 // Device bytes a handle of this configuration takes from an arena: fields and
 // their buffers, pressure, mask, counts, flags, the parameter block, the
 // pressure keys and, for 16-bit storage, the FP32 transfer staging.
@@ -178,6 +182,7 @@ size_t handle_footprint(const os_config& c) {
   auto r = [](size_t b) { return (b + 255) / 256 * 256; };
   size_t bytes = 6 * r(N * e) + 3 * r(N * 4) + r(N) + r(sizeof(StepParams)) + r(2 * sizeof(int));
   if (c.storage != OS_STORAGE_F32) bytes += r(N * 4);
+  bytes += r(kDiagBytes);
   return bytes;
 }
 
@@ -203,6 +208,8 @@ void dev_free(os_handle* h, void* p) {
 
 // The temporally blocked projection/diffusion engine works on the handle.
 #include "os_blocked.cuh"
+// FP64 divergence-residual and conservation sums.
+#include "os_diag.cuh"
 
 namespace {
 
@@ -520,7 +527,7 @@ void free_handle(os_handle* h) {
   if (!h) return;
   if (h->graph) cudaGraphExecDestroy(h->graph);
   void* ptrs[] = {h->u, h->v, h->s, h->ub, h->vb, h->sb, h->p, h->is_solid,
-                  h->total_s, h->flags, h->d_params, h->d_pkeys, h->conv};
+                  h->total_s, h->flags, h->d_params, h->d_pkeys, h->conv, h->diag};
   for (void* q : ptrs) dev_free(h, q);
   if (h->arena_block) h->arena->release(h->arena_block);
   if (h->h_pkeys) cudaFreeHost(h->h_pkeys);
@@ -855,6 +862,55 @@ int os_download(os_handle* h, int32_t field, void* host, size_t count) {
     CUDA_OR_RETURN(cudaMemcpyAsync(host, h->conv, h->N * 4, cudaMemcpyDeviceToHost, h->stream));
   }
   CUDA_OR_RETURN(cudaStreamSynchronize(h->stream));
+  return OS_OK;
+}
+
+int os_diagnose(os_handle* h, os_diag* out) {
+  if (!h || !out) return set_err(OS_ERR_INVALID, "null argument");
+  static_assert(kDiagBytes == (kDiagBlocks + 1) * kDiagSlots * sizeof(double),
+                "diagnostics scratch size");
+  int rc = select_device(h);
+  if (rc) return rc;
+  if (!h->diag) CUDA_OR_RETURN(dev_alloc(h, (void**)&h->diag, kDiagBytes));
+  double* partials = h->diag;
+  double* res = h->diag + (size_t)kDiagBlocks * kDiagSlots;
+  const int64_t need = ((int64_t)h->N + kDiagThreads - 1) / kDiagThreads;
+  const int blocks = (int)std::min<int64_t>(kDiagBlocks, std::max<int64_t>(1, need));
+  const uint8_t* fl = h->flags;
+  switch (h->storage) {
+    case OS_STORAGE_F32:
+      k_diag_partial<float><<<blocks, kDiagThreads, 0, h->stream>>>(
+          (const float*)h->u, (const float*)h->v, (const float*)h->s, fl, h->c, partials);
+      break;
+    case OS_STORAGE_F16:
+      k_diag_partial<__half><<<blocks, kDiagThreads, 0, h->stream>>>(
+          (const __half*)h->u, (const __half*)h->v, (const __half*)h->s, fl, h->c, partials);
+      break;
+    case OS_STORAGE_BF16:
+      k_diag_partial<__nv_bfloat16><<<blocks, kDiagThreads, 0, h->stream>>>(
+          (const __nv_bfloat16*)h->u, (const __nv_bfloat16*)h->v, (const __nv_bfloat16*)h->s,
+          fl, h->c, partials);
+      break;
+    default:
+      k_diag_partial<double><<<blocks, kDiagThreads, 0, h->stream>>>(
+          (const double*)h->u, (const double*)h->v, (const double*)h->s, fl, h->c, partials);
+      break;
+  }
+  k_diag_final<<<1, kDiagThreads, 0, h->stream>>>(partials, blocks, res);
+  h->launches += 2;
+  CUDA_OR_RETURN(cudaGetLastError());
+  double v[kDiagSlots];
+  CUDA_OR_RETURN(cudaMemcpyAsync(v, res, sizeof v, cudaMemcpyDeviceToHost, h->stream));
+  CUDA_OR_RETURN(cudaStreamSynchronize(h->stream));
+  const double cs = (double)h->c.h;
+  memset(out, 0, sizeof *out);
+  out->divergence_l2 = sqrt(v[0]);
+  out->divergence_sum = v[1];
+  out->divergence_max = v[kDiagSums];
+  out->smoke_mass = v[2] * cs * cs;
+  out->inflow_flux = v[3] * cs;
+  out->outflow_flux = v[4] * cs;
+  out->active_cells = (int64_t)v[5];
   return OS_OK;
 }
 

@@ -250,6 +250,13 @@ class Fluid:
         check(self._lib.os_pressure_range(self._h, C.byref(lo), C.byref(hi)))
         return hi.value
 
+    def diagnose(self) -> dict:
+        """FP64 divergence residual (l2, max, sum over the projected cells),
+        smoke mass and inflow/outflow fluxes of the current fields."""
+        d = native.OsDiag()
+        check(self._lib.os_diagnose(self._h, C.byref(d)))
+        return {name: getattr(d, name) for name, _ in native.OsDiag._fields_ if name != "reserved"}
+
     @property
     def kernel_launches(self) -> int:
         out = C.c_int64()

@@ -124,6 +124,7 @@ SIGNATURES = [
                                    C.c_int32, C.c_void_p, C.POINTER(C.c_float),
                                    C.POINTER(C.c_int32)]),
     ("os_diffuse_noalloc", C.c_int, [C.POINTER(OsConfig), C.c_void_p, C.c_float, C.c_void_p]),
+    ("os_diagnose", C.c_int, [C.c_void_p, C.c_void_p]),
     ("os_batch_create", C.c_int, [C.POINTER(OsConfig), C.c_int32, C.c_int32,
                                   C.POINTER(C.c_void_p)]),
     ("os_batch_create_dynamic", C.c_int, [C.c_int32, C.c_int32, C.c_uint64,
@@ -143,6 +144,19 @@ SIGNATURES = [
     ("os_batch_scenario", C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_void_p)]),
     ("os_batch_info", C.c_int, [C.c_void_p, C.c_void_p]),
 ]
+
+
+class OsDiag(C.Structure):
+    _fields_ = [
+        ("divergence_l2", C.c_double),
+        ("divergence_max", C.c_double),
+        ("divergence_sum", C.c_double),
+        ("smoke_mass", C.c_double),
+        ("inflow_flux", C.c_double),
+        ("outflow_flux", C.c_double),
+        ("active_cells", C.c_int64),
+        ("reserved", C.c_int64),
+    ]
 
 
 class OsBatchStats(C.Structure):

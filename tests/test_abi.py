@@ -43,11 +43,13 @@ def _c_layout() -> dict:
 #include "opensayal_gb300.h"
 #define F(s, m) printf(#s "." #m " %zu\n", offsetof(s, m));
 int main(void) {
-  printf("os_config %zu\nos_source %zu\nos_fields_view %zu\nos_batch_stats %zu\n",
-         sizeof(os_config), sizeof(os_source), sizeof(os_fields_view), sizeof(os_batch_stats));
+  printf("os_config %zu\nos_source %zu\nos_fields_view %zu\nos_batch_stats %zu\nos_diag %zu\n",
+         sizeof(os_config), sizeof(os_source), sizeof(os_fields_view), sizeof(os_batch_stats),
+         sizeof(os_diag));
   F(os_config, viscosity) F(os_config, storage) F(os_config, idw_mode)
   F(os_config, obstacle_radius) F(os_source, position_y) F(os_fields_view, total_s)
   F(os_batch_stats, members_in_plan) F(os_batch_stats, steps_completed)
+  F(os_diag, outflow_flux) F(os_diag, active_cells)
   return 0;
 }
 '''
@@ -68,13 +70,16 @@ def test_ctypes_mirror_matches_c_layout():
     assert lay["os_source"] == C.sizeof(native.OsSource)
     assert lay["os_fields_view"] == C.sizeof(native.OsFieldsView)
     assert lay["os_batch_stats"] == C.sizeof(native.OsBatchStats)
+    assert lay["os_diag"] == C.sizeof(native.OsDiag)
     for key, cls in [("os_config.viscosity", native.OsConfig), ("os_config.storage", native.OsConfig),
                      ("os_config.idw_mode", native.OsConfig),
                      ("os_config.obstacle_radius", native.OsConfig),
                      ("os_source.position_y", native.OsSource),
                      ("os_fields_view.total_s", native.OsFieldsView),
                      ("os_batch_stats.members_in_plan", native.OsBatchStats),
-                     ("os_batch_stats.steps_completed", native.OsBatchStats)]:
+                     ("os_batch_stats.steps_completed", native.OsBatchStats),
+                     ("os_diag.outflow_flux", native.OsDiag),
+                     ("os_diag.active_cells", native.OsDiag)]:
         field = key.split(".")[1]
         assert lay[key] == getattr(cls, field).offset, key
 

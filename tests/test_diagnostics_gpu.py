@@ -1,0 +1,102 @@
+"""FP64 diagnostics (os_diagnose): the divergence residual and the smoke-mass
+and flux sums agree with the same quantities computed in FP64 by numpy on the
+downloaded fields, repeat bit for bit, and behave as the scheme implies: the
+residual falls as the projection runs more sweeps, and smoke stays within
+[0, max(1, wind_tunnel.smoke)]."""
+import numpy as np
+import pytest
+
+from opensayal_gb300 import native, scenarios
+from opensayal_gb300.fluid import Fluid, default_config
+from tests.parity_cases import perturbed_state
+
+pytestmark = pytest.mark.gpu
+
+
+def numpy_diag(cfg, f: Fluid) -> dict:
+    """The diagnostics from downloaded fields, in FP64 (reference layout:
+    row r = H-1-j holds cells (0..W-1, j))."""
+    W, H, h = cfg.width, cfg.height, float(int(cfg.cell_size))
+    u = f.download("vel_x").astype(np.float64).reshape(H, W)[::-1]  # [j, i]
+    v = f.download("vel_y").astype(np.float64).reshape(H, W)[::-1]
+    s = f.download("smoke").astype(np.float64).reshape(H, W)[::-1]
+    fluid = (f.download("is_solid").reshape(H, W)[::-1] == 0)
+    active = np.zeros_like(fluid)
+    active[1:H - 1, 1:W - 1] = fluid[1:H - 1, 1:W - 1]
+    d = np.zeros((H, W))
+    d[1:H - 1, 1:W - 1] = ((u[1:H - 1, 2:W] - u[1:H - 1, 1:W - 1]) + v[2:H, 1:W - 1]) \
+        - v[1:H - 1, 1:W - 1]
+    d = np.where(active, d, 0.0)
+    out_mask = fluid[:, W - 1] & fluid[:, W - 2]
+    return {
+        "divergence_l2": float(np.sqrt((d * d).sum())),
+        "divergence_max": float(np.abs(d).max()),
+        "divergence_sum": float(d.sum()),
+        "smoke_mass": float(np.where(fluid, s, 0.0).sum()) * h * h,
+        "inflow_flux": float(np.where(fluid[:, 1] & fluid[:, 2], u[:, 2], 0.0).sum()) * h,
+        "outflow_flux": float(np.where(out_mask, u[:, W - 1], 0.0).sum()) * h,
+        "active_cells": int(active.sum()),
+    }
+
+
+def advanced(cfg, steps, seed=3):
+    f = Fluid(cfg)
+    for k, a in perturbed_state(cfg, seed).items():
+        f.upload(k, a)
+    for _ in range(steps):
+        f.update(None, cfg.d_t)
+    return f
+
+
+@pytest.mark.parametrize("storage", [0, 1, 2, 3])
+def test_diagnostics_match_numpy_fp64(gpu, storage):
+    cfg = scenarios.small_config()
+    cfg.storage = storage
+    cfg.enable_drain = 1
+    with advanced(cfg, 12) as f:
+        got = f.diagnose()
+        want = numpy_diag(cfg, f)
+    assert got["active_cells"] == want["active_cells"]
+    # FP32/FP16/BF16 values are exact in the FP32 download, so only the
+    # summation order differs; FP64 storage is rounded by the download.
+    tol = 1e-12 if storage != 3 else 1e-6
+    for k in ("divergence_l2", "smoke_mass", "inflow_flux", "outflow_flux"):
+        assert got[k] == pytest.approx(want[k], rel=tol, abs=1e-12), k
+    assert got["divergence_sum"] == pytest.approx(want["divergence_sum"], rel=1e-9, abs=1e-9)
+    if storage != 3:
+        assert got["divergence_max"] == want["divergence_max"]
+    assert got["inflow_flux"] > 0 and got["smoke_mass"] > 0
+
+
+def test_diagnostics_repeat_bit_for_bit(gpu):
+    cfg = scenarios.small_config()
+    with advanced(cfg, 5) as f:
+        a, b = f.diagnose(), f.diagnose()
+    assert a == b
+
+
+def test_residual_falls_with_sweeps(gpu):
+    base = scenarios.small_config()
+    state = perturbed_state(base, 9)
+    residual = []
+    for n in (2, 10, 50, 200):
+        cfg = base.copy()
+        cfg.projection_n = n
+        with Fluid(cfg) as f:
+            for k, a in state.items():
+                f.upload(k, a)
+            f.run_phase(native.PHASE_FORCES, None, cfg.d_t)
+            before = f.diagnose()["divergence_l2"]
+            f.run_phase(native.PHASE_PROJECTION, None, cfg.d_t)
+            residual.append(f.diagnose()["divergence_l2"])
+    assert residual[0] < before
+    assert all(b < a for a, b in zip(residual, residual[1:])), residual
+
+
+def test_smoke_stays_in_range(gpu):
+    cfg = default_config(160, 96)
+    cfg.tunnel_smoke = 0.8
+    cfg.projection_n = 20
+    with advanced(cfg, 60) as f:
+        s = f.download("smoke")
+    assert s.min() >= 0.0 and s.max() <= max(1.0, cfg.tunnel_smoke)
