@@ -195,6 +195,8 @@ def run_gb300(args, world, rank, local) -> dict | None:
     cfg.device = local
     if args.block is not None:
         cfg.projection_block = args.block
+    if args.resident is not None:
+        cfg.projection_resident = args.resident
     cells = cfg.width * cfg.height
     f = Fluid(cfg)
     u, v = scenarios.perturbation(2, f.download("is_solid"))
@@ -254,7 +256,8 @@ def run_gb300(args, world, rank, local) -> dict | None:
     traffic = None
     tfile = ROOT / "profiles" / "roofline_traffic.json"
     if tfile.exists():
-        key = f"{args.workload}:block{f.fields().projection_block}"
+        key = f"{args.workload}:block{f.fields().projection_block}" + (
+            ":resident" if f.fields().projection_resident else "")
         traffic = json.loads(tfile.read_text()).get(key)
     step_bytes = bytes_per_cell_step(cfg.projection_n, cfg.viscosity != 0.0)
     ms_per_step = total_s * 1e3 / args.steps
@@ -267,6 +270,7 @@ def run_gb300(args, world, rank, local) -> dict | None:
             "parallelism": "replicas" if world > 1 else "single", "global_batch": world,
             "kernels_per_step": launches // max(1, args.steps),
             "projection_block": f.fields().projection_block,
+            "projection_resident": f.fields().projection_resident,
             "projection_block_source": "autotuned" if cfg.projection_block == 0 else "fixed"}),
         "e2e": e2e,
         "gpu_launches": int(launches),
@@ -581,6 +585,9 @@ def main():
     ap.add_argument("--block", type=int, default=None,
                     help="red/black sweeps per blocked pass (0 autotune, -1 plain)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--resident", type=int, default=None, choices=[-1, 0, 1],
+                    help="projection as one resident cooperative launch: -1 never, 1 when it "
+                         "fits, 0 autotuner decides")
     ap.add_argument("--mixed", action="store_true",
                     help="batched: BF16 storage for half of the scenarios")
     ap.add_argument("--serve-rate", type=float, default=200.0)

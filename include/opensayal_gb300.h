@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define OS_ABI_VERSION 2
+#define OS_ABI_VERSION 3
 
 typedef enum os_status {
   OS_OK = 0,
@@ -119,7 +119,14 @@ typedef struct os_config {
                                690-693): 0 (default) FP32 float-pair
                                arithmetic that rounds like the FP64
                                expression; 1 literal FP64; 2 plain FP32 */
-  int32_t reserved[4];
+  int32_t projection_resident; /* the projection phase as one cooperative
+                               launch whose tiles stay in shared memory and
+                               exchange halos between passes: 0 = the
+                               autotuner decides (with projection_block 0;
+                               a fixed projection_block runs pass by pass);
+                               1 = whenever the grid fits one co-resident tile
+                               per SM and projection_block is even; -1 = never */
+  int32_t reserved[3];
 } os_config;
 
 /* The reference's `Source` (inc/fluid.cuh:8-13), the interactive forcing. */
@@ -143,6 +150,8 @@ typedef struct os_fields_view {
   float* pressure;    /* Fluid::d_pressure */
   int32_t* is_solid;  /* Fluid::d_is_solid */
   int32_t* total_s;   /* Fluid::d_total_s */
+  int32_t projection_resident; /* 1: the resident projection is in use */
+  int32_t reserved;
 } os_fields_view;
 
 typedef struct os_handle os_handle;
@@ -254,6 +263,16 @@ int os_profile_phase(os_handle* h, int32_t phase, const os_source* src, float dt
  * (other streams, or other threads) race on it and must be serialised.
  */
 int os_diffuse_noalloc(const os_config* cfg, float* u, float dt, void* stream);
+
+/*
+ * Failure detection of the resident projection's inter-tile waits, without a
+ * fault: one CTA waits on a neighbour flag that nothing sets. Every such wait
+ * is bounded; when it gives up it records the failure, and the host call that
+ * synchronises reports OS_ERR_TIMEOUT. *status receives what that path
+ * reports here (OS_ERR_TIMEOUT when the bound works). No reference
+ * counterpart.
+ */
+int os_selftest_bounded_wait(int32_t device, int32_t* status);
 
 /*
  * FP64 diagnostics of the current fields (no reference counterpart). The

