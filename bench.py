@@ -585,9 +585,9 @@ def main():
     ap.add_argument("--block", type=int, default=None,
                     help="red/black sweeps per blocked pass (0 autotune, -1 plain)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--resident", type=int, default=None, choices=[-1, 0, 1],
-                    help="projection as one resident cooperative launch: -1 never, 1 when it "
-                         "fits, 0 autotuner decides")
+    ap.add_argument("--resident", type=int, default=None, choices=[-1, 0, 1, 2, 3],
+                    help="phases as resident cooperative launches: mask 1 projection, "
+                         "2 diffusion, 3 both; -1 never; 0 autotuner decides")
     ap.add_argument("--mixed", action="store_true",
                     help="batched: BF16 storage for half of the scenarios")
     ap.add_argument("--serve-rate", type=float, default=200.0)

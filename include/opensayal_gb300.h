@@ -119,13 +119,15 @@ typedef struct os_config {
                                690-693): 0 (default) FP32 float-pair
                                arithmetic that rounds like the FP64
                                expression; 1 literal FP64; 2 plain FP32 */
-  int32_t projection_resident; /* the projection phase as one cooperative
-                               launch whose tiles stay in shared memory and
-                               exchange halos between passes: 0 = the
-                               autotuner decides (with projection_block 0;
-                               a fixed projection_block runs pass by pass);
-                               1 = whenever the grid fits one co-resident tile
-                               per SM and projection_block is even; -1 = never */
+  int32_t projection_resident; /* phases run as one cooperative launch each,
+                               tiles kept in shared memory and exchanging
+                               halos between passes: a mask, 1 the
+                               projection, 2 the diffusion, 3 both, each
+                               where the grid fits one co-resident tile per
+                               SM (projection: projection_block even;
+                               diffusion: a multiple of 4); 0 = the autotuner
+                               decides (with projection_block 0; a fixed
+                               projection_block runs pass by pass); -1 = never */
   int32_t reserved[3];
 } os_config;
 
@@ -150,7 +152,8 @@ typedef struct os_fields_view {
   float* pressure;    /* Fluid::d_pressure */
   int32_t* is_solid;  /* Fluid::d_is_solid */
   int32_t* total_s;   /* Fluid::d_total_s */
-  int32_t projection_resident; /* 1: the resident projection is in use */
+  int32_t projection_resident; /* resident forms in use: bit 0 projection,
+                                  bit 1 diffusion */
   int32_t reserved;
 } os_fields_view;
 

@@ -453,14 +453,13 @@ k_project_blocked(const S* __restrict__ u_in, const S* __restrict__ v_in,
 // ---------------------------------------------------------------------------
 // Blocked Jacobi diffusion of u.
 // ---------------------------------------------------------------------------
-template <class S>
-__device__ __forceinline__ void diffuse_tile(float* smem, int tx, int ty,
-                                             const S* __restrict__ u_in, S* __restrict__ u_out,
-                                             const Consts& c, const StepParams* __restrict__ prm,
-                                             int sweeps, int halo, int TX, int TY) {
+// The region of tile (tx, ty) into both buffers A and B (cells that no sweep
+// updates keep their value in each).
+template <class S, bool CG = false>
+__device__ __forceinline__ void diff_stage_in(float* A, float* B, int tx, int ty,
+                                              const S* __restrict__ u_in, const Consts& c,
+                                              int halo, int TX, int TY) {
   const int RH = TY + 2 * halo;
-  float* A = smem;
-  float* B = smem + RH * kRegionW + kArrPad;
   const int gx0 = tx * TX - halo, gy0 = ty * TY - halo;
   const int W = c.W, H = c.H;
   const bool vec = ((W & 3) == 0) && ((gx0 & 3) == 0);
@@ -471,19 +470,31 @@ __device__ __forceinline__ void diffuse_tile(float* smem, int tx, int ty,
     for (int r = 0; r < kInFlight; r++) {
       const int it = base + r * blockDim.x;
       const int y = it / kQuads, x = 4 * (it % kQuads);
-      uq[r] = it < items ? load_quad(u_in, W, H, gx0 + x, gy0 + y, vec)
-                         : make_float4(0.f, 0.f, 0.f, 0.f);
+      const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (CG)
+        uq[r] = it < items ? load_quad_cg(u_in, W, H, gx0 + x, gy0 + y, vec) : z;
+      else
+        uq[r] = it < items ? load_quad(u_in, W, H, gx0 + x, gy0 + y, vec) : z;
     }
 #pragma unroll
     for (int r = 0; r < kInFlight; r++) {
       const int it = base + r * blockDim.x;
       if (it >= items) break;
-      // Both buffers: cells that no sweep updates keep their value in each.
       *reinterpret_cast<float4*>(A + 4 * it) = uq[r];
       *reinterpret_cast<float4*>(B + 4 * it) = uq[r];
     }
   }
-  __syncthreads();
+}
+
+// `sweeps` Jacobi sweeps on the staged region, A -> B -> A ...; on return A
+// holds the result (the pointers are swapped as the sweeps go). Ends with a
+// barrier.
+__device__ __forceinline__ void diff_sweeps(float*& A, float*& B, int tx, int ty, const Consts& c,
+                                            const StepParams* __restrict__ prm, int sweeps,
+                                            int halo, int TX, int TY) {
+  const int RH = TY + 2 * halo;
+  const int gx0 = tx * TX - halo, gy0 = ty * TY - halo;
+  const int W = c.W, H = c.H;
   const float d_t = prm->dt;
   const float a = c.viscosity * d_t / (float)(c.h * c.h);
   // Updated cells: domain interior and not on the region's outer ring. A
@@ -519,6 +530,16 @@ __device__ __forceinline__ void diffuse_tile(float* smem, int tx, int ty,
     A = B;
     B = T;
   }
+}
+
+// Owned cells of the region in A back to global.
+template <class S>
+__device__ __forceinline__ void diff_store_owned(const float* A, int tx, int ty,
+                                                 S* __restrict__ u_out, const Consts& c, int halo,
+                                                 int TX, int TY) {
+  const int gx0 = tx * TX - halo, gy0 = ty * TY - halo;
+  const int W = c.W, H = c.H;
+  const bool vec = ((W & 3) == 0) && ((gx0 & 3) == 0);
   for (int it = threadIdx.x; it < TY * kQuads; it += blockDim.x) {
     const int y = halo + it / kQuads, x = 4 * (it % kQuads);
     const int i = gx0 + x, j = gy0 + y;
@@ -533,6 +554,20 @@ __device__ __forceinline__ void diffuse_tile(float* smem, int tx, int ty,
       st(u_out + cell_index(W, H, i + d, j), src[d]);
     }
   }
+}
+
+template <class S>
+__device__ __forceinline__ void diffuse_tile(float* smem, int tx, int ty,
+                                             const S* __restrict__ u_in, S* __restrict__ u_out,
+                                             const Consts& c, const StepParams* __restrict__ prm,
+                                             int sweeps, int halo, int TX, int TY) {
+  const int RH = TY + 2 * halo;
+  float* A = smem;
+  float* B = smem + RH * kRegionW + kArrPad;
+  diff_stage_in<S>(A, B, tx, ty, u_in, c, halo, TX, TY);
+  __syncthreads();
+  diff_sweeps(A, B, tx, ty, c, prm, sweeps, halo, TX, TY);
+  diff_store_owned<S>(A, tx, ty, u_out, c, halo, TX, TY);
 }
 
 template <class S>

@@ -159,8 +159,10 @@ struct os_handle {
   double* diag = nullptr;   // diagnostics partials and result (first use)
   // Resident projection (one cooperative launch per phase): tile flags, the
   // device error word, and a mapped host word the kernel sets on a failed wait.
-  int resident = 0;
+  int resident = 0;       // projection
+  int resident_diff = 0;  // diffusion
   unsigned* rflags = nullptr;
+  unsigned* dflags = nullptr;
   int* rerr = nullptr;
   int* host_rerr = nullptr;
   int* d_host_rerr = nullptr;
@@ -267,6 +269,15 @@ constexpr bool kBlockedTypes = std::is_same<A, float>::value &&
 template <class S, class A>
 void enqueue_diffusion(os_handle* h, Vel<S>& w, Enq& q) {
   if constexpr (kBlockedTypes<S, A>) {
+    if (use_blocked<S, A>(h) && h->resident_diff) {
+      const int n = enqueue_resident_diffusion<S>(h, q.st, &w.cu);
+      if (n > 0) {
+        q.count += n;
+        return;
+      }
+      q.failed = true;
+      return;
+    }
     if (use_blocked<S, A>(h)) {
       q.count += enqueue_blocked_diffusion<S>(h, q.st, &w.cu);
       return;
@@ -532,8 +543,8 @@ int validate(const os_config* c) {
     return set_err(OS_ERR_INVALID, "thread.cuda.block_size_* must be >= 1");
   if (storage_bytes(c->storage) == 0) return set_err(OS_ERR_INVALID, "unknown storage %d", c->storage);
   if (c->idw_mode < 0 || c->idw_mode > 2) return set_err(OS_ERR_INVALID, "idw_mode must be 0, 1 or 2");
-  if (c->projection_resident < -1 || c->projection_resident > 1)
-    return set_err(OS_ERR_INVALID, "projection_resident must be -1, 0 or 1");
+  if (c->projection_resident < -1 || c->projection_resident > 3)
+    return set_err(OS_ERR_INVALID, "projection_resident must be -1, 0, 1, 2 or 3");
   if (c->smoke_count != 1) {
     if (c->smoke_count - 1 == 0) return set_err(OS_ERR_INVALID, "smoke_count");
     const int spacing = (c->pipe_height - c->smoke_count * c->smoke_height) / (c->smoke_count - 1);
@@ -551,39 +562,46 @@ struct TuneChoice {
 };
 TuneChoice autotune_projection(const os_config& base);
 
-// Sets up the resident projection (flags, error words) when the grid fits it.
-int enable_resident(os_handle* h) {
+// Sets up the resident projection (mask bit 0) and diffusion (bit 1) that
+// the grid fits (flags, error words).
+int enable_resident(os_handle* h, int mask) {
   if (h->block_k <= 0 || h->storage == OS_STORAGE_F64 || h->arena) return OS_OK;
   const bool pressure = h->cfg.enable_pressure != 0;
   const int sms = sm_count(h->cfg.device);
-  TileGeom g;
-  if (!resident_geom(h->W, h->H, h->block_k, pressure, sms, &g)) return OS_OK;
-  bool ok = false;
+  TileGeom g, gd;
+  bool proj = (mask & 1) && resident_geom(h->W, h->H, h->block_k, pressure, sms, &g);
+  bool diff = (mask & 2) && resident_diffusion_geom(h->W, h->H, h->block_k, sms, &gd);
   switch (h->storage) {
     case OS_STORAGE_F32:
-      ok = pressure ? resident_launchable<true, float>(g, sms) : resident_launchable<false, float>(g, sms);
+      proj = proj && (pressure ? resident_launchable<true, float>(g, sms)
+                               : resident_launchable<false, float>(g, sms));
+      diff = diff && resident_diffusion_launchable<float>(gd, sms);
       break;
     case OS_STORAGE_F16:
-      ok = pressure ? resident_launchable<true, __half>(g, sms)
-                    : resident_launchable<false, __half>(g, sms);
+      proj = proj && (pressure ? resident_launchable<true, __half>(g, sms)
+                               : resident_launchable<false, __half>(g, sms));
+      diff = diff && resident_diffusion_launchable<__half>(gd, sms);
       break;
     case OS_STORAGE_BF16:
-      ok = pressure ? resident_launchable<true, __nv_bfloat16>(g, sms)
-                    : resident_launchable<false, __nv_bfloat16>(g, sms);
+      proj = proj && (pressure ? resident_launchable<true, __nv_bfloat16>(g, sms)
+                               : resident_launchable<false, __nv_bfloat16>(g, sms));
+      diff = diff && resident_diffusion_launchable<__nv_bfloat16>(gd, sms);
       break;
   }
-  if (!ok) {
-    cudaGetLastError();
-    return OS_OK;
-  }
-  CUDA_OR_RETURN(cudaMalloc(&h->rflags, (size_t)sms * sizeof(unsigned)));
-  CUDA_OR_RETURN(cudaMemset(h->rflags, 0, (size_t)sms * sizeof(unsigned)));
+  cudaGetLastError();
+  if (!proj && !diff) return OS_OK;
+  const size_t fb = (size_t)sms * sizeof(unsigned);
+  CUDA_OR_RETURN(cudaMalloc(&h->rflags, fb));
+  CUDA_OR_RETURN(cudaMemset(h->rflags, 0, fb));
+  CUDA_OR_RETURN(cudaMalloc(&h->dflags, fb));
+  CUDA_OR_RETURN(cudaMemset(h->dflags, 0, fb));
   CUDA_OR_RETURN(cudaMalloc(&h->rerr, sizeof(int)));
   CUDA_OR_RETURN(cudaMemset(h->rerr, 0, sizeof(int)));
   CUDA_OR_RETURN(cudaHostAlloc(&h->host_rerr, sizeof(int), cudaHostAllocMapped));
   *h->host_rerr = 0;
   CUDA_OR_RETURN(cudaHostGetDevicePointer((void**)&h->d_host_rerr, h->host_rerr, 0));
-  h->resident = 1;
+  h->resident = proj;
+  h->resident_diff = diff;
   return OS_OK;
 }
 
@@ -595,11 +613,12 @@ int check_resident(os_handle* h) {
   *(volatile int*)h->host_rerr = 0;
   const int sms = sm_count(h->cfg.device);
   cudaMemsetAsync(h->rflags, 0, (size_t)sms * sizeof(unsigned), h->stream);
+  cudaMemsetAsync(h->dflags, 0, (size_t)sms * sizeof(unsigned), h->stream);
   cudaMemsetAsync(h->rerr, 0, sizeof(int), h->stream);
   cudaStreamSynchronize(h->stream);
   return set_err(OS_ERR_TIMEOUT,
-                 "resident projection: a tile gave up waiting for its neighbours; the fields "
-                 "are undefined");
+                 "resident projection or diffusion: a tile gave up waiting for its "
+                 "neighbours; the fields are undefined");
 }
 
 void free_handle(os_handle* h) {
@@ -612,6 +631,7 @@ void free_handle(os_handle* h) {
   if (h->h_pkeys) cudaFreeHost(h->h_pkeys);
   if (h->h_params) cudaFreeHost(h->h_params);
   if (h->rflags) cudaFree(h->rflags);
+  if (h->dflags) cudaFree(h->dflags);
   if (h->rerr) cudaFree(h->rerr);
   if (h->host_rerr) cudaFreeHost(h->host_rerr);
   if (h->params_event) cudaEventDestroy(h->params_event);
@@ -823,18 +843,18 @@ static int create_handle(const os_config* cfg, Arena* arena, os_handle** out) {
   if ((e = cudaGetLastError()) != cudaSuccess ||
       (e = cudaStreamSynchronize(h->stream)) != cudaSuccess)
     return fail(set_err(OS_ERR_CUDA, "init: %s", cudaGetErrorString(e)));
-  bool resident = cfg->projection_resident == 1;
+  int resident = cfg->projection_resident > 0 ? cfg->projection_resident : 0;
   if (h->block_k == 0) {
     if (h->storage == OS_STORAGE_F64) {
       h->block_k = -1;
     } else {
       const TuneChoice t = autotune_projection(*cfg);
       h->block_k = t.K;
-      resident = t.resident != 0;
+      resident = t.resident;
     }
   }
   if (resident) {
-    const int rc = enable_resident(h);
+    const int rc = enable_resident(h, resident);
     if (rc) return fail(rc);
   }
   *out = h;
@@ -904,7 +924,7 @@ int os_fields(os_handle* h, os_fields_view* out) {
   out->pressure = h->p;
   out->is_solid = h->is_solid;
   out->total_s = h->total_s;
-  out->projection_resident = h->resident;
+  out->projection_resident = (h->resident ? 1 : 0) | (h->resident_diff ? 2 : 0);
   return OS_OK;
 }
 
@@ -1147,12 +1167,15 @@ float time_steps(os_handle* t, float dt, int warm, int reps) {
 }
 
 // Candidates: depths {2, 4, 6, 8, 12} pass by pass and, unless
-// projection_resident is -1, depths {2, 4, 6, 8} resident (where the grid
-// fits); projection_resident 1 restricts the search to the resident form.
+// projection_resident is -1, the resident forms the depth allows (projection
+// for even depths, diffusion for multiples of 4, alone or together) where
+// the grid fits them; a positive projection_resident fixes the forms and
+// leaves only the depth to choose.
 TuneChoice autotune_projection(const os_config& base) {
   constexpr TuneChoice kDefault{4, 0};
   const char* env = std::getenv("OPENSAYAL_GB300_AUTOTUNE");
-  if (env && env[0] == '0') return TuneChoice{kDefault.K, base.projection_resident == 1};
+  if (env && env[0] == '0')
+    return TuneChoice{kDefault.K, base.projection_resident > 0 ? base.projection_resident : 0};
   const TuneKey key{base.width, base.height, base.projection_n, base.viscosity != 0.0f,
                     base.enable_pressure != 0, base.storage, base.device,
                     base.projection_resident};
@@ -1162,10 +1185,19 @@ TuneChoice autotune_projection(const os_config& base) {
     if (it != g_tuned.end()) return it->second;
   }
   std::vector<TuneChoice> cands;
-  if (base.projection_resident != 1)
-    for (int K : {2, 4, 6, 8, 12}) cands.push_back({K, 0});
-  if (base.projection_resident != -1)
-    for (int K : {2, 4, 6, 8}) cands.push_back({K, 1});
+  for (int K : {2, 4, 6, 8, 12}) {
+    if (base.projection_resident > 0) {
+      cands.push_back({K, base.projection_resident});
+      continue;
+    }
+    cands.push_back({K, 0});
+    if (base.projection_resident == -1) continue;
+    if (K % 2 == 0 && K <= 8) cands.push_back({K, 1});
+    if (K % 4 == 0 && base.viscosity != 0.0f) {
+      cands.push_back({K, 2});
+      if (K <= 8) cands.push_back({K, 3});
+    }
+  }
   const float dt = base.d_t > 0.0f ? base.d_t : 0.05f;
   TuneChoice best = kDefault;
   float best_ms = 0.0f;
@@ -1173,14 +1205,15 @@ TuneChoice autotune_projection(const os_config& base) {
     if (cand.K > std::max(1, base.projection_n)) continue;
     os_config c = base;
     c.projection_block = cand.K;
-    c.projection_resident = cand.resident ? 1 : -1;
+    c.projection_resident = cand.resident ? cand.resident : -1;
     os_handle* t = nullptr;
     if (os_create(&c, &t) != OS_OK) continue;  // e.g. out of memory: skip
-    if (cand.resident && !t->resident) {        // grid does not fit the form
+    const int got = (t->resident ? 1 : 0) | (t->resident_diff ? 2 : 0);
+    if (got != cand.resident) {  // the grid does not fit that form
       os_destroy(t);
       continue;
     }
-    const float ms = time_steps(t, dt, 2, 3);
+    const float ms = time_steps(t, dt, 3, 12);
     os_destroy(t);
     if (ms > 0.0f && (best_ms == 0.0f || ms < best_ms)) {
       best_ms = ms;

@@ -39,6 +39,17 @@ __device__ __forceinline__ void st_release_gpu(unsigned* p, unsigned v) {
   asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
+// Publishes this CTA's pass: the barrier orders every thread's band stores
+// before thread 0's fence, whose release ordering (cumulative over what the
+// barrier made visible to it) precedes the flag store.
+__device__ __forceinline__ void publish_flag(unsigned* flag, unsigned v) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    asm volatile("fence.acq_rel.gpu;" ::: "memory");
+    st_release_gpu(flag, v);
+  }
+}
+
 // Region cell (y, quad q) of the halo ring for flat index `it`: the top rows
 // [0, halo), the bottom rows [halo + TY, RH) (full width), then the left and
 // right quads [0, hq) and [kQuads - hq, kQuads) of the owned rows.
@@ -180,7 +191,7 @@ __device__ __forceinline__ bool wait_neighbours(const ResidentSync& S, int tx, i
       }
     }
   }
-  __threadfence();
+  // The acquire loads order the reloads that follow the barrier.
   __syncthreads();
   return give_up == 0;
 }
@@ -217,16 +228,120 @@ k_project_resident(S* U0, S* U1, S* V0, S* V1, int cu, int cv, float* __restrict
     publish_rect<PRESSURE, S>(smem, RH, uo, vo, W, H, gx0, gy0, TY, TY + halo, oq0, oq1, vec);
     publish_rect<PRESSURE, S>(smem, RH, uo, vo, W, H, gx0, gy0, 2 * halo, TY, oq0, oq0 + hq, vec);
     publish_rect<PRESSURE, S>(smem, RH, uo, vo, W, H, gx0, gy0, 2 * halo, TY, oq1 - hq, oq1, vec);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      __threadfence();
-      st_release_gpu(sync.flags + blockIdx.x, epoch + q + 1);
-    }
+    publish_flag(sync.flags + blockIdx.x, epoch + q + 1);
     if (!wait_neighbours(sync, tx, ty, tiles_x, tiles_y, epoch + q + 1)) return;
     // The halo ring from the neighbours' bands; owned cells rounded as the
     // pass engine's write-back would round them.
     round_owned<PRESSURE, S>(smem, RH, halo, TX, TY);
     reload_ring<PRESSURE, S>(smem, RH, uo, vo, W, H, gx0, gy0, halo, TY, vec);
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Resident Jacobi diffusion: the same scheme for apply_diffusion_at
+// (src/fluid.cu:176-183), halo K for K sweeps, on the dense two-buffer region
+// of the pass engine (diff_stage_in / diff_sweeps / diff_store_owned). Only
+// the buffer holding the current sweep's input needs the fresh ring: cells no
+// sweep updates (domain boundary, off the grid) are constant and staged into
+// both buffers at the start.
+// ---------------------------------------------------------------------------
+
+template <class S>
+__device__ __forceinline__ void reload_ring_dense(float* A, const S* __restrict__ u, int W, int H,
+                                                  int gx0, int gy0, int halo, int TY, bool vec) {
+  const int hq = halo / 4;
+  const int items = 2 * halo * kQuads + 2 * TY * hq;
+  for (int base = threadIdx.x; base < items; base += blockDim.x * kInFlight) {
+    float4 uq[kInFlight];
+#pragma unroll
+    for (int r = 0; r < kInFlight; r++) {
+      const int it = base + r * blockDim.x;
+      uq[r] = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (it < items) {
+        int y, q;
+        ring_cell(it, halo, TY, hq, &y, &q);
+        uq[r] = load_quad_cg(u, W, H, gx0 + 4 * q, gy0 + y, vec);
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < kInFlight; r++) {
+      const int it = base + r * blockDim.x;
+      if (it >= items) break;
+      int y, q;
+      ring_cell(it, halo, TY, hq, &y, &q);
+      *reinterpret_cast<float4*>(A + y * kRegionW + 4 * q) = uq[r];
+    }
+  }
+}
+
+// Owned cells within `halo` of the tile's edges, from A to global.
+template <class S>
+__device__ __forceinline__ void publish_band_dense(const float* A, S* __restrict__ u, int W, int H,
+                                                   int gx0, int gy0, int halo, int TX, int TY,
+                                                   bool vec) {
+  const int hq = halo / 4, oq = TX / 4;  // owned quads per row: [hq, hq + oq)
+  const int band = halo * oq, side = (TY - 2 * halo > 0 ? TY - 2 * halo : 0) * hq;
+  const int items = 2 * band + 2 * side;
+  for (int it = threadIdx.x; it < items; it += blockDim.x) {
+    int y, q;
+    if (it < band) {
+      y = halo + it / oq;
+      q = hq + it % oq;
+    } else if (it < 2 * band) {
+      y = TY + (it - band) / oq;
+      q = hq + (it - band) % oq;
+    } else {
+      const int r = it - 2 * band;
+      const int sd = r / side, k = r - sd * side;
+      y = 2 * halo + k / hq;
+      q = (sd ? hq + oq - hq : hq) + k % hq;
+    }
+    const int i = gx0 + 4 * q, j = gy0 + y;
+    if (j >= H || i >= W) continue;
+    store_quad(u, W, H, i, j, vec, *reinterpret_cast<const float4*>(A + y * kRegionW + 4 * q));
+  }
+}
+
+template <class S>
+__device__ __forceinline__ void round_owned_dense(float* A, int halo, int TX, int TY) {
+  if (std::is_same<S, float>::value) return;
+  const S* tag = nullptr;
+  for (int it = threadIdx.x; it < TY * TX; it += blockDim.x) {
+    const int e = (halo + it / TX) * kRegionW + halo + it % TX;
+    A[e] = to_storage_and_back(A[e], tag);
+  }
+}
+
+template <class S>
+__global__ void __launch_bounds__(kBlockThreads, 1)
+k_diffuse_resident(S* U0, S* U1, int cu, Consts c, const StepParams* __restrict__ prm, int K,
+                   int halo, int TX, int TY, int tiles_x, int tiles_y, ResidentSync sync) {
+  extern __shared__ __align__(16) float smem[];
+  const int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
+  const int RH = TY + 2 * halo;
+  const int W = c.W, H = c.H;
+  const int gx0 = tx * TX - halo, gy0 = ty * TY - halo;
+  const bool vec = ((W & 3) == 0) && ((gx0 & 3) == 0);
+  float* A = smem;
+  float* B = smem + RH * kRegionW + kArrPad;
+  const unsigned epoch = ld_acquire_gpu(sync.flags + blockIdx.x);
+  // Through L2: this launch later writes the input copy (X_1).
+  diff_stage_in<S, true>(A, B, tx, ty, cu ? U1 : U0, c, halo, TX, TY);
+  __syncthreads();
+  const int passes = (c.n + K - 1) / K;
+  for (int q = 0; q < passes; q++) {
+    diff_sweeps(A, B, tx, ty, c, prm, min(K, c.n - q * K), halo, TX, TY);
+    S* uo = ((cu + q + 1) & 1) ? U1 : U0;
+    if (q == passes - 1) {
+      diff_store_owned<S>(A, tx, ty, uo, c, halo, TX, TY);
+      return;
+    }
+    publish_band_dense<S>(A, uo, W, H, gx0, gy0, halo, TX, TY, vec);
+    publish_flag(sync.flags + blockIdx.x, epoch + q + 1);
+    if (!wait_neighbours(sync, tx, ty, tiles_x, tiles_y, epoch + q + 1)) return;
+    round_owned_dense<S>(A, halo, TX, TY);
+    reload_ring_dense<S>(A, uo, W, H, gx0, gy0, halo, TY, vec);
     __syncthreads();
   }
 }
@@ -260,6 +375,66 @@ inline bool resident_geom(int W, int H, int K, bool pressure, int sms, TileGeom*
   if (g.smem + 64 > kMaxSmem || g.tiles_x * g.tiles_y > sms) return false;
   *out = g;
   return true;
+}
+
+// The same for the resident diffusion: halo K, K a multiple of 4.
+inline bool resident_diffusion_geom(int W, int H, int K, int sms, TileGeom* out) {
+  if (K < 4 || (K & 3)) return false;
+  TileGeom g;
+  g.halo = K;
+  g.TX = kRegionW - 2 * g.halo;
+  if (g.TX < 2 * g.halo) return false;
+  g.tiles_x = (W + g.TX - 1) / g.TX;
+  const int rows_of_tiles = sms / g.tiles_x;
+  if (rows_of_tiles < 1) return false;
+  int TY = (H + rows_of_tiles - 1) / rows_of_tiles;
+  TY = std::max(2 * g.halo, (TY + 1) & ~1);
+  g.TY = TY;
+  g.RH = TY + 2 * g.halo;
+  g.tiles_y = (H + TY - 1) / TY;
+  g.smem = diffusion_smem(g.RH);
+  if (g.smem + 64 > kMaxSmem || g.tiles_x * g.tiles_y > sms) return false;
+  *out = g;
+  return true;
+}
+
+template <class S>
+inline bool resident_diffusion_launchable(const TileGeom& g, int sms) {
+  auto fn = k_diffuse_resident<S>;
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.smem) !=
+      cudaSuccess)
+    return false;
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kBlockThreads, g.smem) !=
+      cudaSuccess)
+    return false;
+  return per_sm >= 1 && g.tiles_x * g.tiles_y <= per_sm * sms;
+}
+
+template <class S>
+inline int enqueue_resident_diffusion(os_handle* h, cudaStream_t st, int* cur_u) {
+  const int K = h->block_k;
+  TileGeom g;
+  if (!resident_diffusion_geom(h->W, h->H, K, sm_count(h->cfg.device), &g)) return -1;
+  const ResidentSync rs{h->dflags, h->rerr, h->d_host_rerr};
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(g.tiles_x * g.tiles_y);
+  cfg.blockDim = dim3(kBlockThreads);
+  cfg.dynamicSmemBytes = g.smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaFuncSetAttribute(k_diffuse_resident<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)g.smem);
+  const cudaError_t e = cudaLaunchKernelEx(
+      &cfg, k_diffuse_resident<S>, static_cast<S*>(h->u), static_cast<S*>(h->ub), *cur_u, h->c,
+      (const StepParams*)h->d_params, K, g.halo, g.TX, g.TY, g.tiles_x, g.tiles_y, rs);
+  if (e != cudaSuccess) return -1;
+  if (((h->c.n + K - 1) / K) & 1) *cur_u = 1 - *cur_u;
+  return 1;
 }
 
 template <bool PRESSURE, class S>

@@ -36,7 +36,7 @@ def pair(base, state, k):
     resident.projection_resident = 1
     a, b = load_lib(passes, state), load_lib(resident, state)
     assert a.fields().projection_resident == 0
-    if b.fields().projection_resident != 1:
+    if not b.fields().projection_resident & 1:
         a.close()
         b.close()
         pytest.skip("tiles of this size do not fit one per SM in shared memory")
@@ -60,6 +60,32 @@ def test_resident_projection_equals_passes(gpu, w, h, k, pressure):
     b.close()
 
 
+@pytest.mark.parametrize("w,h", SIZES)
+@pytest.mark.parametrize("k", [4, 8, 12])
+def test_resident_diffusion_equals_passes(gpu, w, h, k):
+    base = tunnel(w, h, viscosity=0.02)
+    solid = oracle.OracleFluid(base).is_solid
+    state = random_state(base, 37, solid)
+    passes = base.copy()
+    passes.projection_block = k
+    passes.projection_resident = -1
+    resident = base.copy()
+    resident.projection_block = k
+    resident.projection_resident = 2
+    a, b = load_lib(passes, state), load_lib(resident, state)
+    if not b.fields().projection_resident & 2:
+        a.close()
+        b.close()
+        pytest.skip("tiles of this size do not fit one per SM in shared memory")
+    a.run_phase(native.PHASE_DIFFUSION, None, 0.05)
+    b.run_phase(native.PHASE_DIFFUSION, None, 0.05)
+    for field in FIELDS:
+        x, y = a.download(field), b.download(field)
+        assert same_bits(x, y), f"{field}: {int((x != y).sum())} cells differ"
+    a.close()
+    b.close()
+
+
 @pytest.mark.parametrize("storage", [0, 1, 2])
 def test_resident_steps_equal_plain(gpu, storage):
     cfg = scenarios.default_tunnel_config()
@@ -70,9 +96,9 @@ def test_resident_steps_equal_plain(gpu, storage):
     plain.projection_block = -1
     res = cfg.copy()
     res.projection_block = 4
-    res.projection_resident = 1
+    res.projection_resident = 3
     a, b = load_lib(plain, state), load_lib(res, state)
-    assert b.fields().projection_resident == 1
+    assert b.fields().projection_resident == 3  # projection and diffusion
     for _ in range(6):
         a.update(None, cfg.d_t)
         b.update(None, cfg.d_t)
@@ -101,7 +127,7 @@ def test_resident_falls_back_when_grid_does_not_fit(gpu):
     cfg = scenarios.large_config()
     cfg.projection_n = 8
     cfg.projection_block = 4
-    cfg.projection_resident = 1
+    cfg.projection_resident = 3
     with Fluid(cfg) as f:
         assert f.fields().projection_resident == 0  # 4096 x 4096 needs more tiles than SMs
         f.update(None, cfg.d_t)
@@ -114,7 +140,7 @@ def test_bounded_wait_reports_timeout_and_context_survives(gpu):
     native.check(lib.os_selftest_bounded_wait(0, C.byref(status)))
     assert status.value == native.OS_ERR_TIMEOUT
     # The context is still usable: a resident step runs and is finite.
-    cfg = tunnel(512, 256, projection_block=4, projection_resident=1)
+    cfg = tunnel(512, 256, projection_block=4, projection_resident=3)
     with Fluid(cfg) as f:
         f.update(None, cfg.d_t)
         assert np.isfinite(f.download("vel_x")).all()
