@@ -185,6 +185,44 @@ def config_record(cfg, name: str, extra: dict) -> dict:
     return rec
 
 
+def time_visuals(f, cfg, sptr, stream, pk) -> dict:
+    """Headless visuals on the workload's fields: pixel colours (reads smoke
+    and the flag byte, writes one word: 9 B per cell), and the arrows and path
+    lines at the reference's default spacing; CUDA events, 20 calls each."""
+    import torch
+    from opensayal_gb300.fluid import visual_defaults
+    from opensayal_gb300.native import OsArrow
+    import ctypes as C
+    v = visual_defaults()
+    cells = cfg.width * cfg.height
+    pix = torch.empty(cells, dtype=torch.int32, device="cuda")
+    aw, ah = cfg.width // v.arrow_distance, cfg.height // v.arrow_distance
+    arrows = torch.empty(max(1, aw * ah) * C.sizeof(OsArrow) // 4, dtype=torch.int32, device="cuda")
+    tw, th = cfg.width // v.trace_distance, cfg.height // v.trace_distance
+    tx = torch.empty(max(1, tw * th * v.trace_length), dtype=torch.int32, device="cuda")
+    ty = torch.empty_like(tx)
+    calls = {
+        "pixels": lambda: f.render_pixels(pix.data_ptr(), sptr),
+        "arrows": lambda: f.render_arrows(v, arrows.data_ptr(), sptr),
+        "traces": lambda: f.render_traces(v, cfg.d_t, tx.data_ptr(), ty.data_ptr(), sptr),
+    }
+    out = {}
+    for name, fn in calls.items():
+        fn()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(20):
+            fn()
+        b.record(stream)
+        b.synchronize()
+        out[name + "_us"] = a.elapsed_time(b) / 20 * 1e3
+    gbs = 9 * cells / (out["pixels_us"] * 1e-6) / 1e9
+    out["pixels_gbs"] = gbs
+    out["pixels_frac"] = gbs / pk["hbm_gbs"]
+    out["note"] = "pixels: 9 B/cell (smoke, flag, pixel word); L2-warm back-to-back calls"
+    return out
+
+
 def run_gb300(args, world, rank, local) -> dict | None:
     import torch
     from opensayal_gb300 import Fluid, native, scenarios
@@ -285,6 +323,7 @@ def run_gb300(args, world, rank, local) -> dict | None:
         "wall_s": wall,
         "clocks": clk.summary(),
     }
+    result["visual"] = time_visuals(f, cfg, sptr, stream, pk)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline(cfg)
     f.close()

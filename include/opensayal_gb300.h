@@ -268,6 +268,50 @@ int os_profile_phase(os_handle* h, int32_t phase, const os_source* src, float dt
 int os_diffuse_noalloc(const os_config* cfg, float* u, float dt, void* stream);
 
 /*
+ * Headless visuals: the reference's per-frame colouring, velocity arrows and
+ * path lines (src/graphics_handler.cu:168-396, src/helper.cu, the
+ * `visual.*` and `sim.cell_pixel_size` keys of src/config_parser.cpp:39-40,
+ * 120-179), written to caller-owned device buffers on `stream` (NULL: the
+ * handle's stream) without waiting. No window or graphics library is used.
+ */
+typedef struct os_visual_config {
+  int32_t cell_pixel_size;        /* sim.cell_pixel_size (1) */
+  int32_t arrow_distance;         /* visual.arrows.distance (20) */
+  float arrow_length_multiplier;  /* visual.arrows.length_multiplier (0.1) */
+  float arrow_disable_threshold;  /* visual.arrows.disable_threshold (0) */
+  int32_t arrow_head_length;      /* visual.arrows.head_length (5) */
+  int32_t trace_distance;         /* visual.path_line.distance (20) */
+  int32_t trace_length;           /* visual.path_line.length (20) */
+  int32_t reserved;
+} os_visual_config;
+
+/* The reference's ArrowData (inc/graphics_handler.cuh:17-27), pixel
+ * coordinates; an entry with valid == 0 carries no other data. */
+typedef struct os_arrow {
+  int32_t start_x, start_y, end_x, end_y;
+  int32_t right_head_end_x, right_head_end_y, left_head_end_x, left_head_end_y;
+  int32_t valid;
+} os_arrow;
+
+int os_visual_defaults(os_visual_config* out);
+/* W*H RGBA words (r << 24 | g << 16 | b << 8 | a) at y * W + x for pixel
+ * (x, y) = (i, H - 1 - j), the cell's own index: solid cells grey, the others
+ * coloured by smoke and/or pressure as sim.enable_smoke/enable_pressure say
+ * (pressure normalised by the last update's extrema); with both off, fluid
+ * pixels are left unchanged. */
+int os_render_pixels(os_handle* h, int32_t* d_pixels, void* stream);
+/* (W / d) x (H / d) arrows, d = arrow_distance, entry (a, b) at
+ * (H / d - b - 1) * (W / d) + a for the arrow from cell (a d, b d); entries of
+ * solid cells are left unchanged. */
+int os_render_arrows(os_handle* h, const os_visual_config* v, os_arrow* d_arrows, void* stream);
+/* Path lines of trace_length points from every d-th cell (d = trace_distance),
+ * stepped by `dt`: point k of line (a, b) at
+ * ((H / d - b - 1) * (W / d) + a) * trace_length + k in d_x and d_y; a solid
+ * start cell gets (-1, -1) as its first point only. */
+int os_render_traces(os_handle* h, const os_visual_config* v, float dt, int32_t* d_x,
+                     int32_t* d_y, void* stream);
+
+/*
  * Failure detection of the resident projection's inter-tile waits, without a
  * fault: one CTA waits on a neighbour flag that nothing sets. Every such wait
  * is bounded; when it gives up it records the failure, and the host call that

@@ -221,6 +221,8 @@ void dev_free(os_handle* h, void* p) {
 #include "os_resident.cuh"
 // FP64 divergence-residual and conservation sums.
 #include "os_diag.cuh"
+// Pixel colours, velocity arrows and path lines as device buffers.
+#include "os_visual.cuh"
 
 namespace {
 
@@ -1027,6 +1029,129 @@ int os_diagnose(os_handle* h, os_diag* out) {
   out->inflow_flux = v[3] * cs;
   out->outflow_flux = v[4] * cs;
   out->active_cells = (int64_t)v[5];
+  return OS_OK;
+}
+
+int os_visual_defaults(os_visual_config* out) {
+  if (!out) return set_err(OS_ERR_INVALID, "null argument");
+  memset(out, 0, sizeof *out);
+  out->cell_pixel_size = 1;
+  out->arrow_distance = 20;
+  out->arrow_length_multiplier = 0.1f;
+  out->arrow_disable_threshold = 0.0f;
+  out->arrow_head_length = 5;
+  out->trace_distance = 20;
+  out->trace_length = 20;
+  return OS_OK;
+}
+
+static int visual_params(const os_handle* h, const os_visual_config* v, VisualParams* vp) {
+  if (!v) return set_err(OS_ERR_INVALID, "null visual config");
+  if (v->cell_pixel_size < 1 || v->arrow_distance < 1 || v->trace_distance < 1 ||
+      v->trace_length < 1)
+    return set_err(OS_ERR_INVALID, "visual distances, lengths and pixel size must be >= 1");
+  memset(vp, 0, sizeof *vp);
+  vp->cell_px = v->cell_pixel_size;
+  vp->arrow_distance = v->arrow_distance;
+  vp->arrow_length_multiplier = v->arrow_length_multiplier;
+  vp->arrow_disable_threshold = v->arrow_disable_threshold;
+  vp->arrow_head_length = (float)v->arrow_head_length;
+  vp->arrow_head_angle = (float)(M_PI / 8);  // ARROW_HEAD_ANGLE, inc/config.hpp:6
+  vp->arrows_w = h->W / v->arrow_distance;
+  vp->arrows_h = h->H / v->arrow_distance;
+  vp->trace_distance = v->trace_distance;
+  vp->trace_length = v->trace_length;
+  vp->traces_w = h->W / v->trace_distance;
+  vp->traces_h = h->H / v->trace_distance;
+  return OS_OK;
+}
+
+int os_render_pixels(os_handle* h, int32_t* d_pixels, void* stream) {
+  if (!h || !d_pixels) return set_err(OS_ERR_INVALID, "null argument");
+  int rc = select_device(h);
+  if (rc) return rc;
+  cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : h->stream;
+  const dim3 g((h->W + 127) / 128, h->H);
+  const int ep = h->cfg.enable_pressure != 0, es = h->cfg.enable_smoke != 0;
+  switch (h->storage) {
+    case OS_STORAGE_F32:
+      k_render_pixels<float><<<g, 128, 0, st>>>((const float*)h->s, h->p, h->flags, h->c, ep, es,
+                                                h->min_pressure, h->max_pressure, d_pixels);
+      break;
+    case OS_STORAGE_F16:
+      k_render_pixels<__half><<<g, 128, 0, st>>>((const __half*)h->s, h->p, h->flags, h->c, ep,
+                                                 es, h->min_pressure, h->max_pressure, d_pixels);
+      break;
+    case OS_STORAGE_BF16:
+      k_render_pixels<__nv_bfloat16><<<g, 128, 0, st>>>((const __nv_bfloat16*)h->s, h->p,
+                                                        h->flags, h->c, ep, es, h->min_pressure,
+                                                        h->max_pressure, d_pixels);
+      break;
+    default:
+      return set_err(OS_ERR_UNSUPPORTED, "visuals need FP32, FP16 or BF16 storage");
+  }
+  h->launches++;
+  CUDA_OR_RETURN(cudaGetLastError());
+  return OS_OK;
+}
+
+int os_render_arrows(os_handle* h, const os_visual_config* v, os_arrow* d_arrows, void* stream) {
+  if (!h || !d_arrows) return set_err(OS_ERR_INVALID, "null argument");
+  VisualParams vp;
+  int rc = visual_params(h, v, &vp);
+  if (rc || (rc = select_device(h))) return rc;
+  if (vp.arrows_w < 1 || vp.arrows_h < 1) return OS_OK;
+  cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : h->stream;
+  const dim3 b(16, 16), g((vp.arrows_w + 15) / 16, (vp.arrows_h + 15) / 16);
+  switch (h->storage) {
+    case OS_STORAGE_F32:
+      k_render_arrows<float><<<g, b, 0, st>>>((const float*)h->u, (const float*)h->v, h->flags,
+                                              h->c, vp, d_arrows);
+      break;
+    case OS_STORAGE_F16:
+      k_render_arrows<__half><<<g, b, 0, st>>>((const __half*)h->u, (const __half*)h->v,
+                                               h->flags, h->c, vp, d_arrows);
+      break;
+    case OS_STORAGE_BF16:
+      k_render_arrows<__nv_bfloat16><<<g, b, 0, st>>>(
+          (const __nv_bfloat16*)h->u, (const __nv_bfloat16*)h->v, h->flags, h->c, vp, d_arrows);
+      break;
+    default:
+      return set_err(OS_ERR_UNSUPPORTED, "visuals need FP32, FP16 or BF16 storage");
+  }
+  h->launches++;
+  CUDA_OR_RETURN(cudaGetLastError());
+  return OS_OK;
+}
+
+int os_render_traces(os_handle* h, const os_visual_config* v, float dt, int32_t* d_x,
+                     int32_t* d_y, void* stream) {
+  if (!h || !d_x || !d_y) return set_err(OS_ERR_INVALID, "null argument");
+  VisualParams vp;
+  int rc = visual_params(h, v, &vp);
+  if (rc || (rc = select_device(h))) return rc;
+  if (vp.traces_w < 1 || vp.traces_h < 1) return OS_OK;
+  cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : h->stream;
+  const dim3 b(16, 16), g((vp.traces_w + 15) / 16, (vp.traces_h + 15) / 16);
+  switch (h->storage) {
+    case OS_STORAGE_F32:
+      k_render_traces<float><<<g, b, 0, st>>>((const float*)h->u, (const float*)h->v, h->flags,
+                                              h->c, vp, dt, d_x, d_y);
+      break;
+    case OS_STORAGE_F16:
+      k_render_traces<__half><<<g, b, 0, st>>>((const __half*)h->u, (const __half*)h->v,
+                                               h->flags, h->c, vp, dt, d_x, d_y);
+      break;
+    case OS_STORAGE_BF16:
+      k_render_traces<__nv_bfloat16><<<g, b, 0, st>>>((const __nv_bfloat16*)h->u,
+                                                      (const __nv_bfloat16*)h->v, h->flags, h->c,
+                                                      vp, dt, d_x, d_y);
+      break;
+    default:
+      return set_err(OS_ERR_UNSUPPORTED, "visuals need FP32, FP16 or BF16 storage");
+  }
+  h->launches++;
+  CUDA_OR_RETURN(cudaGetLastError());
   return OS_OK;
 }
 

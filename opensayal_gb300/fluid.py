@@ -102,6 +102,14 @@ def _convert(value: Any, typ: type, key: str) -> Any:
     return int(value) if typ is int else float(value)
 
 
+def visual_defaults() -> native.OsVisualConfig:
+    """The `visual.*` and `sim.cell_pixel_size` defaults of
+    src/config_parser.cpp:39-40, 120-179."""
+    v = native.OsVisualConfig()
+    check(native.load().os_visual_defaults(C.byref(v)))
+    return v
+
+
 def load_config(source: dict | str | Path) -> OsConfig:
     """Parse an OpenSayal.conf.json (path, JSON text or dict) with the reference's
     defaults and dotted-key lookup. Size-dependent defaults (pipe and smoke
@@ -249,6 +257,23 @@ class Fluid:
         lo, hi = C.c_float(), C.c_float()
         check(self._lib.os_pressure_range(self._h, C.byref(lo), C.byref(hi)))
         return hi.value
+
+    # Headless visuals into caller-owned device buffers (device pointers as
+    # integers, e.g. a torch tensor's data_ptr()); enqueued without waiting.
+    def render_pixels(self, d_pixels: int, stream: int | None = None) -> None:
+        check(self._lib.os_render_pixels(self._h, C.c_void_p(d_pixels),
+                                         C.c_void_p(stream) if stream else None))
+
+    def render_arrows(self, visual: "native.OsVisualConfig", d_arrows: int,
+                      stream: int | None = None) -> None:
+        check(self._lib.os_render_arrows(self._h, C.byref(visual), C.c_void_p(d_arrows),
+                                         C.c_void_p(stream) if stream else None))
+
+    def render_traces(self, visual: "native.OsVisualConfig", d_t: float, d_x: int, d_y: int,
+                      stream: int | None = None) -> None:
+        check(self._lib.os_render_traces(self._h, C.byref(visual), C.c_float(d_t),
+                                         C.c_void_p(d_x), C.c_void_p(d_y),
+                                         C.c_void_p(stream) if stream else None))
 
     def diagnose(self) -> dict:
         """FP64 divergence residual (l2, max, sum over the projected cells),

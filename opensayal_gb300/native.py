@@ -128,6 +128,11 @@ SIGNATURES = [
                                    C.POINTER(C.c_int32)]),
     ("os_diffuse_noalloc", C.c_int, [C.POINTER(OsConfig), C.c_void_p, C.c_float, C.c_void_p]),
     ("os_diagnose", C.c_int, [C.c_void_p, C.c_void_p]),
+    ("os_visual_defaults", C.c_int, [C.c_void_p]),
+    ("os_render_pixels", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("os_render_arrows", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("os_render_traces", C.c_int, [C.c_void_p, C.c_void_p, C.c_float, C.c_void_p, C.c_void_p,
+                                   C.c_void_p]),
     ("os_selftest_bounded_wait", C.c_int, [C.c_int32, C.POINTER(C.c_int32)]),
     ("os_batch_create", C.c_int, [C.POINTER(OsConfig), C.c_int32, C.c_int32,
                                   C.POINTER(C.c_void_p)]),
@@ -161,6 +166,25 @@ class OsDiag(C.Structure):
         ("active_cells", C.c_int64),
         ("reserved", C.c_int64),
     ]
+
+
+class OsVisualConfig(C.Structure):
+    _fields_ = [
+        ("cell_pixel_size", C.c_int32),
+        ("arrow_distance", C.c_int32),
+        ("arrow_length_multiplier", C.c_float),
+        ("arrow_disable_threshold", C.c_float),
+        ("arrow_head_length", C.c_int32),
+        ("trace_distance", C.c_int32),
+        ("trace_length", C.c_int32),
+        ("reserved", C.c_int32),
+    ]
+
+
+class OsArrow(C.Structure):
+    _fields_ = [(name, C.c_int32) for name in (
+        "start_x", "start_y", "end_x", "end_y", "right_head_end_x", "right_head_end_y",
+        "left_head_end_x", "left_head_end_y", "valid")]
 
 
 class OsBatchStats(C.Structure):

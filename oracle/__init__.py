@@ -20,6 +20,7 @@ HERE = Path(__file__).resolve().parent
 ORACLE_SO = HERE / "build" / "liboracle.so"
 HARNESS_SO = HERE / "build" / "libref_harness.so"
 REF_CUBIN = HERE / "_ref" / "fluid_ref.cubin"
+VISUAL_CUBIN = HERE / "_ref" / "visual_ref.cubin"
 
 # The reference's x86-64 g++ 13 -O3 build starts the uninitialised diffusion
 # loop counter (src/fluid.cu:186) at zero: n diffusion sweeps per step.
@@ -157,9 +158,17 @@ def _load_harness():
         lib.ref_phase.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_float, C.c_int]
         lib.ref_update.argtypes = [C.c_void_p, C.c_void_p, C.c_float, C.c_int]
         lib.ref_pressure_range.argtypes = [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float)]
+        lib.ref_visual_open.argtypes = [C.c_char_p]
+        lib.ref_render_pixels.argtypes = [C.c_void_p, C.c_float, C.c_float, C.c_void_p]
+        lib.ref_render_traces.argtypes = [C.c_void_p, C.c_float, C.c_int, C.c_int, C.c_void_p,
+                                          C.c_void_p]
+        lib.ref_render_arrows.argtypes = [C.c_void_p, C.c_int, C.c_float, C.c_float, C.c_float,
+                                          C.c_float, C.c_int, C.c_void_p]
         rc = lib.ref_open(str(REF_CUBIN).encode())
         if rc != 0:
             raise RuntimeError(f"reference cubin: {lib.ref_last_error().decode()}")
+        if VISUAL_CUBIN.exists() and lib.ref_visual_open(str(VISUAL_CUBIN).encode()) != 0:
+            raise RuntimeError(f"visual cubin: {lib.ref_last_error().decode()}")
         _harness = lib
     return _harness
 
@@ -233,6 +242,37 @@ class RefFluid:
         lo, hi = C.c_float(), C.c_float()
         self.lib.ref_pressure_range(self.h, C.byref(lo), C.byref(hi))
         return lo.value, hi.value
+
+    # Visuals (ref_visual.cu): `init` arrays are the buffers' prior contents.
+    def render_pixels(self, min_pressure: float, max_pressure: float, init: np.ndarray) -> np.ndarray:
+        out = np.ascontiguousarray(init, dtype=np.int32).copy()
+        if self.lib.ref_render_pixels(self.h, min_pressure, max_pressure,
+                                      out.ctypes.data_as(C.c_void_p)):
+            raise RuntimeError(self.lib.ref_last_error().decode())
+        return out
+
+    def render_traces(self, dt: float, distance: int, length: int, init_x: np.ndarray,
+                      init_y: np.ndarray):
+        xs = np.ascontiguousarray(init_x, dtype=np.int32).copy()
+        ys = np.ascontiguousarray(init_y, dtype=np.int32).copy()
+        if self.lib.ref_render_traces(self.h, dt, distance, length, xs.ctypes.data_as(C.c_void_p),
+                                      ys.ctypes.data_as(C.c_void_p)):
+            raise RuntimeError(self.lib.ref_last_error().decode())
+        return xs, ys
+
+    def render_arrows(self, cell_size: int, length_multiplier: float, disable_threshold: float,
+                      head_length: float, head_angle: float, distance: int,
+                      init: np.ndarray) -> np.ndarray:
+        """ArrowData records as an (n, 9) int32 array; column 8 is `valid` (its
+        first byte; the padding bytes are masked off)."""
+        raw = np.ascontiguousarray(init, dtype=np.int32).copy()
+        if self.lib.ref_render_arrows(self.h, cell_size, length_multiplier, disable_threshold,
+                                      head_length, head_angle, distance,
+                                      raw.ctypes.data_as(C.c_void_p)):
+            raise RuntimeError(self.lib.ref_last_error().decode())
+        raw = raw.reshape(-1, 9)
+        raw[:, 8] &= 0xFF
+        return raw
 
 
 def rel_l2(a: np.ndarray, b: np.ndarray) -> float:

@@ -348,4 +348,83 @@ int ref_pressure_range(void* h, float* mn, float* mx) {
   return 0;
 }
 
+// ---------------------------------------------------------------------------
+// Visuals: oracle/_ref/visual_ref.cubin (ref_visual.cu linked with the
+// reference's fluid.cu and helper.cu). Each call copies `inout` to a device
+// buffer, runs the kernel on the handle's Fluid and copies the buffer back,
+// so entries a kernel leaves alone keep the caller's values.
+// ---------------------------------------------------------------------------
+
+cudaLibrary_t g_vlib = nullptr;
+cudaKernel_t g_vpixels, g_vtraces, g_varrows;
+
+int ref_visual_open(const char* cubin_path) {
+  if (g_vlib) return 0;
+  cudaError_t e = cudaLibraryLoadFromFile(&g_vlib, cubin_path, nullptr, nullptr, 0, nullptr,
+                                          nullptr, 0);
+  if (e != cudaSuccess) return fail("cudaLibraryLoadFromFile(visual)", e);
+  if ((e = cudaLibraryGetKernel(&g_vpixels, g_vlib, "ref_pixels")) != cudaSuccess ||
+      (e = cudaLibraryGetKernel(&g_vtraces, g_vlib, "ref_traces")) != cudaSuccess ||
+      (e = cudaLibraryGetKernel(&g_varrows, g_vlib, "ref_arrows")) != cudaSuccess)
+    return fail("visual kernels", e);
+  return 0;
+}
+
+static int run_inout(const void* kernel, dim3 grid, dim3 block, void** args, void* dbuf,
+                     void* inout, size_t bytes) {
+  cudaError_t e = cudaMemcpy(dbuf, inout, bytes, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaLaunchKernel(kernel, grid, block, args, 0, (cudaStream_t)0);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(inout, dbuf, bytes, cudaMemcpyDeviceToHost);
+  return e == cudaSuccess ? 0 : fail("visual kernel", e);
+}
+
+int ref_render_pixels(void* h, float min_pressure, float max_pressure, int32_t* inout) {
+  Ref* r = static_cast<Ref*>(h);
+  const size_t bytes = r->cells * sizeof(int32_t);
+  int32_t* d = nullptr;
+  if (cudaMalloc(&d, bytes) != cudaSuccess) return fail("cudaMalloc", cudaErrorMemoryAllocation);
+  void* args[] = {&r->d_this, &d, &min_pressure, &max_pressure};
+  const dim3 block(16, 16), grid((r->f.width + 15) / 16, (r->f.height + 15) / 16);
+  const int rc = run_inout((const void*)g_vpixels, grid, block, args, d, inout, bytes);
+  cudaFree(d);
+  return rc;
+}
+
+int ref_render_traces(void* h, float dt, int distance, int length, int32_t* xs, int32_t* ys) {
+  Ref* r = static_cast<Ref*>(h);
+  int tw = r->f.width / distance, th = r->f.height / distance;
+  if (tw < 1 || th < 1) return 0;
+  const size_t bytes = (size_t)tw * th * length * sizeof(int32_t);
+  int32_t *dx = nullptr, *dy = nullptr;
+  if (cudaMalloc(&dx, bytes) != cudaSuccess || cudaMalloc(&dy, bytes) != cudaSuccess)
+    return fail("cudaMalloc", cudaErrorMemoryAllocation);
+  cudaMemcpy(dy, ys, bytes, cudaMemcpyHostToDevice);
+  void* args[] = {&r->d_this, &dt, &dx, &dy, &distance, &length, &tw, &th};
+  const dim3 block(16, 16), grid((tw + 15) / 16, (th + 15) / 16);
+  int rc = run_inout((const void*)g_vtraces, grid, block, args, dx, xs, bytes);
+  if (!rc && cudaMemcpy(ys, dy, bytes, cudaMemcpyDeviceToHost) != cudaSuccess)
+    rc = fail("copy traces", cudaErrorUnknown);
+  cudaFree(dx);
+  cudaFree(dy);
+  return rc;
+}
+
+// `inout`: (W / d) * (H / d) ArrowData records of 36 bytes.
+int ref_render_arrows(void* h, int cell_size, float length_multiplier, float disable_threshold,
+                      float head_length, float head_angle, int distance, void* inout) {
+  Ref* r = static_cast<Ref*>(h);
+  int aw = r->f.width / distance, ah = r->f.height / distance;
+  if (aw < 1 || ah < 1) return 0;
+  const size_t bytes = (size_t)aw * ah * 36;
+  void* d = nullptr;
+  if (cudaMalloc(&d, bytes) != cudaSuccess) return fail("cudaMalloc", cudaErrorMemoryAllocation);
+  void* args[] = {&r->d_this, &d, &cell_size, &length_multiplier, &disable_threshold,
+                  &head_length, &head_angle, &distance, &aw, &ah};
+  const dim3 block(16, 16), grid((aw + 15) / 16, (ah + 15) / 16);
+  const int rc = run_inout((const void*)g_varrows, grid, block, args, d, inout, bytes);
+  cudaFree(d);
+  return rc;
+}
+
 }  // extern "C"

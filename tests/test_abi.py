@@ -147,3 +147,13 @@ def test_null_arguments_are_errors(lib_built):
     assert lib.os_destroy(None) == native.OS_OK
     assert lib.os_config_defaults(16, 16, None) == native.OS_ERR_INVALID
     assert lib.os_fields(None, None) == native.OS_ERR_INVALID
+
+
+def test_visual_defaults_follow_config_parser(lib_built):
+    # src/config_parser.cpp:39-40, 120-179
+    from opensayal_gb300.fluid import visual_defaults
+    v = visual_defaults()
+    assert (v.cell_pixel_size, v.arrow_distance, v.arrow_head_length) == (1, 20, 5)
+    assert (v.trace_distance, v.trace_length) == (20, 20)
+    assert abs(v.arrow_length_multiplier - 0.1) < 1e-7 and v.arrow_disable_threshold == 0.0
+    assert C.sizeof(native.OsArrow) == 36 and C.sizeof(native.OsVisualConfig) == 32
