@@ -375,6 +375,8 @@ typedef struct os_batch_stats {
   int64_t tile_items_per_step;
   int64_t steps_enqueued;     /* batch steps enqueued so far */
   int64_t steps_completed;    /* of those, seen complete by the host */
+  int32_t projection_tile_rows; /* owned rows of a projection tile */
+  int32_t diffusion_tile_rows;  /* owned rows of a diffusion tile */
 } os_batch_stats;
 
 typedef enum os_member_state {
@@ -384,9 +386,13 @@ typedef enum os_member_state {
 } os_member_state;
 
 /* A batch of fixed members, each stepping until the batch is destroyed; member
- * ids are 0..count-1. `block_k`: sweeps per blocked pass (0 = 8, at most 16). */
+ * ids are 0..count-1. `block_k`: sweeps per blocked pass (at most 16); 0 =
+ * autotune: times a few steps of depths {4, 6, 8, 12} and two tile heights on
+ * the new members (whose fields start at zero and are zeroed again), keeping
+ * the fastest. */
 int os_batch_create(const os_config* cfgs, int32_t count, int32_t block_k, os_batch** out);
-/* An empty batch on `device` for continuous batching. `budget_bytes` > 0
+/* An empty batch on `device` for continuous batching (`block_k` 0 = 8).
+ * `budget_bytes` > 0
  * reserves that much device memory for the members (0: each member allocates
  * its own, without a limit). */
 int os_batch_create_dynamic(int32_t device, int32_t block_k, uint64_t budget_bytes,

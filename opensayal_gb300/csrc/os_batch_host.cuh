@@ -32,6 +32,7 @@ struct os_batch {
   };
   int device = 0;
   int K = 8;
+  int ty_div = 1;  // tile height: the largest that fits, divided by this
   int sms = 152;
   cudaStream_t stream = nullptr;
   Arena* arena = nullptr;  // null: members allocate with cudaMalloc
@@ -69,8 +70,10 @@ struct os_batch {
 
 namespace {
 
-// Largest even tile height whose region fits shared memory.
-TileGeom batch_geom(int halo, bool projection) {
+// Largest even tile height whose region fits shared memory, divided by
+// `ty_div` (rounded to even): shorter tiles balance better across the SMs at
+// the price of more halo rows.
+TileGeom batch_geom(int halo, bool projection, int ty_div = 1) {
   TileGeom g{};
   g.halo = halo;
   g.TX = kRegionW - 2 * halo;
@@ -79,9 +82,10 @@ TileGeom batch_geom(int halo, bool projection) {
     const int next = TY + 2;
     const size_t sm = projection ? projection_smem(next + 2 * halo, false)
                                  : diffusion_smem(next + 2 * halo);
-    if (sm > kMaxSmem) break;
+    if (sm + 256 > kMaxSmem) break;  // room for the kernels' static shared memory
     TY = next;
   }
+  TY = std::max(2, (TY / std::max(1, ty_div)) & ~1);
   g.TY = TY;
   g.RH = TY + 2 * halo;
   g.smem = projection ? projection_smem(g.RH, false) : diffusion_smem(g.RH);
@@ -392,6 +396,84 @@ int batch_progress(os_batch* b) {
   return OS_OK;
 }
 
+// Blocking depth and tile height for the whole batch; the plan and graph are
+// rewritten at the next step.
+int set_geometry(os_batch* b, int K, int ty_div) {
+  if (b->graph) {
+    CUDA_OR_RETURN(cudaStreamSynchronize(b->stream));
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+  }
+  b->graph_dpasses = b->graph_ppasses = -1;
+  b->K = K;
+  b->ty_div = ty_div;
+  b->gd = batch_geom(K, false, ty_div);
+  b->gp = batch_geom(2 * K, true, ty_div);
+  cudaFuncSetAttribute(k_batch_diffuse, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)b->gd.smem);
+  cudaFuncSetAttribute(k_batch_project, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)b->gp.smem);
+  for (auto& kv : b->members) {
+    kv.second.h->block_k = K;
+    kv.second.h->cfg.projection_block = K;
+  }
+  b->dirty = true;
+  CUDA_OR_RETURN(cudaGetLastError());
+  return OS_OK;
+}
+
+int write_plan(os_batch* b, cudaStream_t st);
+
+// Autotuner of a fixed batch: times a few steps of every blocking depth and
+// tile height on the members' freshly created (all-zero) fields, keeps the
+// fastest, and zeroes the fields again, so the members start exactly as
+// os_create leaves them.
+int tune_batch(os_batch* b) {
+  struct Cand {
+    int K, div;
+  };
+  std::vector<Cand> cands;
+  for (int K : {4, 6, 8, 12})
+    for (int div : {1, 2}) cands.push_back({K, div});
+  int max_n = 0;
+  for (auto& kv : b->members) max_n = std::max(max_n, kv.second.h->c.n);
+  cudaEvent_t a = nullptr, z = nullptr;
+  CUDA_OR_RETURN(cudaEventCreate(&a));
+  CUDA_OR_RETURN(cudaEventCreate(&z));
+  Cand best{b->K, b->ty_div};
+  float best_ms = 0.0f;
+  int rc = OS_OK;
+  for (const Cand& cd : cands) {
+    if ((max_n + cd.K - 1) / cd.K > kBatchMaxPasses) continue;
+    if ((rc = set_geometry(b, cd.K, cd.div)) || (rc = write_plan(b, b->stream))) break;
+    CUDA_OR_RETURN(cudaGraphLaunch(b->graph, b->stream));  // warm-up
+    cudaEventRecord(a, b->stream);
+    for (int t = 0; t < 3; t++) CUDA_OR_RETURN(cudaGraphLaunch(b->graph, b->stream));
+    cudaEventRecord(z, b->stream);
+    CUDA_OR_RETURN(cudaEventSynchronize(z));
+    float ms = 0.0f;
+    CUDA_OR_RETURN(cudaEventElapsedTime(&ms, a, z));
+    b->launches += 4LL * b->kernels_per_step;
+    if (best_ms == 0.0f || ms < best_ms) {
+      best_ms = ms;
+      best = cd;
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(z);
+  if (rc) return rc;
+  if ((rc = set_geometry(b, best.K, best.div)) || (rc = write_plan(b, b->stream))) return rc;
+  for (auto& kv : b->members) {
+    os_handle* h = kv.second.h;
+    const size_t fb = h->N * h->esize;
+    void* fields[] = {h->u, h->v, h->s, h->ub, h->vb, h->sb};
+    for (void* f : fields) CUDA_OR_RETURN(cudaMemsetAsync(f, 0, fb, b->stream));
+    CUDA_OR_RETURN(cudaMemsetAsync(h->p, 0, h->N * 4, b->stream));
+  }
+  CUDA_OR_RETURN(cudaStreamSynchronize(b->stream));
+  return OS_OK;
+}
+
 int new_batch(int device, int block_k, uint64_t budget, os_batch** out) {
   os_batch* b = new (std::nothrow) os_batch();
   if (!b) return set_err(OS_ERR_NOMEM, "host allocation failed");
@@ -499,6 +581,11 @@ int os_batch_create(const os_config* cfgs, int32_t count, int32_t block_k, os_ba
     }
   }
   if ((rc = write_plan(b, b->stream))) {
+    free_batch(b);
+    return rc;
+  }
+  const char* env = std::getenv("OPENSAYAL_GB300_AUTOTUNE");
+  if (block_k == 0 && !(env && env[0] == '0') && (rc = tune_batch(b))) {
     free_batch(b);
     return rc;
   }
@@ -694,6 +781,8 @@ int os_batch_info(os_batch* b, os_batch_stats* out) {
   out->tile_items_per_step = b->plan_tiles;
   out->steps_enqueued = b->steps_enqueued;
   out->steps_completed = b->steps_done;
+  out->projection_tile_rows = b->gp.TY;
+  out->diffusion_tile_rows = b->gd.TY;
   return OS_OK;
 }
 

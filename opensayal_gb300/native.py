@@ -198,6 +198,8 @@ class OsBatchStats(C.Structure):
         ("tile_items_per_step", C.c_int64),
         ("steps_enqueued", C.c_int64),
         ("steps_completed", C.c_int64),
+        ("projection_tile_rows", C.c_int32),
+        ("diffusion_tile_rows", C.c_int32),
     ]
 
 

@@ -70,7 +70,10 @@ def test_batch_of_generated_scenarios_runs(gpu):
         for i in range(len(cfgs)):
             s = b.scenario(i).download("smoke")
             assert np.isfinite(s).all()
-        assert b.stats().kernels_per_step < 60
+        st = b.stats()
+        passes = -(-max(c.projection_n for c in cfgs) // st.block_k)
+        assert st.kernels_per_step == 2 * passes + 6
+        assert st.block_k in (4, 6, 8, 12) and st.projection_tile_rows >= 2
 
 
 def test_batch_rejects_pressure(gpu):
