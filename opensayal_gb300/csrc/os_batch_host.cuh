@@ -82,7 +82,7 @@ TileGeom batch_geom(int halo, bool projection, int ty_div = 1) {
     const int next = TY + 2;
     const size_t sm = projection ? projection_smem(next + 2 * halo, false)
                                  : diffusion_smem(next + 2 * halo);
-    if (sm + 256 > kMaxSmem) break;  // room for the kernels' static shared memory
+    if (sm + kStaticSmem > kMaxSmem) break;  // room for the kernels' static shared memory
     TY = next;
   }
   TY = std::max(2, (TY / std::max(1, ty_div)) & ~1);

@@ -205,7 +205,10 @@ __device__ __forceinline__ ProjPlanes proj_planes(float* smem, int RH) {
 // plane offset, is fixed for the whole loop. Planes are addressed as word
 // offsets from the __shared__ base: ue 0, uo 1, ve 2, vo 3, pe 4, po 5 (x plane).
 // apply_projection_at (src/fluid.cu:229-262) for one cell given its four faces
-// and flag byte; faces it may not touch come back unchanged.
+// and flag byte; faces it may not touch come back unchanged. (A table of the
+// reciprocals of s in shared memory gives the same bits as the fast-math
+// division, but measured slower: shared-memory traffic, not the reciprocal,
+// binds these sweeps.)
 template <bool PRESSURE>
 __device__ __forceinline__ void project_faces(uint32_t f, const Consts& c, float d_t, float& uc,
                                               float& right_u, float& vc, float& top_v,
@@ -585,6 +588,7 @@ k_diffuse_blocked(const S* __restrict__ u_in, S* __restrict__ u_out, Consts c,
 // ---------------------------------------------------------------------------
 
 constexpr size_t kMaxSmem = 227 * 1024;
+constexpr size_t kStaticSmem = 256;
 
 // Owned tile height for a given halo: aim for one CTA per SM per wave
 // (152 SMs), keep TY even (region origin parity), and fit shared memory.
@@ -600,7 +604,8 @@ inline TileGeom make_geom(int W, int H, int halo, bool projection, bool pressure
     const int rh = ty + 2 * halo;
     return projection ? projection_smem(rh, pressure) : diffusion_smem(rh);
   };
-  while (TY > 2 && smem_of(TY) > kMaxSmem) TY -= 2;
+  // kStaticSmem: room for the kernels' own static shared memory.
+  while (TY > 2 && smem_of(TY) + kStaticSmem > kMaxSmem) TY -= 2;
   g.TY = TY;
   g.RH = TY + 2 * halo;
   g.tiles_y = (H + TY - 1) / TY;

@@ -372,7 +372,7 @@ inline bool resident_geom(int W, int H, int K, bool pressure, int sms, TileGeom*
   g.tiles_y = (H + TY - 1) / TY;
   g.smem = projection_smem(g.RH, pressure);
   // Static shared memory of the kernel (the wait flag) sits beside the region.
-  if (g.smem + 64 > kMaxSmem || g.tiles_x * g.tiles_y > sms) return false;
+  if (g.smem + kStaticSmem > kMaxSmem || g.tiles_x * g.tiles_y > sms) return false;
   *out = g;
   return true;
 }
@@ -393,7 +393,7 @@ inline bool resident_diffusion_geom(int W, int H, int K, int sms, TileGeom* out)
   g.RH = TY + 2 * g.halo;
   g.tiles_y = (H + TY - 1) / TY;
   g.smem = diffusion_smem(g.RH);
-  if (g.smem + 64 > kMaxSmem || g.tiles_x * g.tiles_y > sms) return false;
+  if (g.smem + kStaticSmem > kMaxSmem || g.tiles_x * g.tiles_y > sms) return false;
   *out = g;
   return true;
 }
