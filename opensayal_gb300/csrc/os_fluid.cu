@@ -1071,21 +1071,24 @@ int os_render_pixels(os_handle* h, int32_t* d_pixels, void* stream) {
   int rc = select_device(h);
   if (rc) return rc;
   cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : h->stream;
-  const dim3 g((h->W + 127) / 128, h->H);
+  const int64_t n = (int64_t)h->N;
+  const unsigned g = (unsigned)((n + 4 * 128 - 1) / (4 * 128));
   const int ep = h->cfg.enable_pressure != 0, es = h->cfg.enable_smoke != 0;
+  // Field arrays come from cudaMalloc or the arena (256-byte aligned).
+  const int vec = (reinterpret_cast<uintptr_t>(d_pixels) % 16) == 0;
   switch (h->storage) {
     case OS_STORAGE_F32:
-      k_render_pixels<float><<<g, 128, 0, st>>>((const float*)h->s, h->p, h->flags, h->c, ep, es,
-                                                h->min_pressure, h->max_pressure, d_pixels);
+      k_render_pixels<float><<<g, 128, 0, st>>>((const float*)h->s, h->p, h->flags, n, ep, es,
+                                                h->min_pressure, h->max_pressure, d_pixels, vec);
       break;
     case OS_STORAGE_F16:
-      k_render_pixels<__half><<<g, 128, 0, st>>>((const __half*)h->s, h->p, h->flags, h->c, ep,
-                                                 es, h->min_pressure, h->max_pressure, d_pixels);
+      k_render_pixels<__half><<<g, 128, 0, st>>>((const __half*)h->s, h->p, h->flags, n, ep, es,
+                                                 h->min_pressure, h->max_pressure, d_pixels, vec);
       break;
     case OS_STORAGE_BF16:
       k_render_pixels<__nv_bfloat16><<<g, 128, 0, st>>>((const __nv_bfloat16*)h->s, h->p,
-                                                        h->flags, h->c, ep, es, h->min_pressure,
-                                                        h->max_pressure, d_pixels);
+                                                        h->flags, n, ep, es, h->min_pressure,
+                                                        h->max_pressure, d_pixels, vec);
       break;
     default:
       return set_err(OS_ERR_UNSUPPORTED, "visuals need FP32, FP16 or BF16 storage");

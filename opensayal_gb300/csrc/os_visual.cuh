@@ -43,23 +43,14 @@ __device__ __forceinline__ void vis_hsv_to_rgb(float h, float s, float v, uint8_
   b = static_cast<uint8_t>((bb + m) * 255);
 }
 
-// update_fluid_pixels_kernel (src/graphics_handler.cu:262-287) with its three
-// colourings (:214-260). Pixel (x, y) = (i, H - 1 - j) is stored at y * W + x,
-// the cell's own index. Cells that are neither solid nor coloured (smoke and
-// pressure both off) are left as they are.
-template <class S>
-__global__ void k_render_pixels(const S* __restrict__ smoke, const float* __restrict__ pressure,
-                                const uint8_t* __restrict__ fl, Consts c, int enable_pressure,
-                                int enable_smoke, float min_pressure, float max_pressure,
-                                int* __restrict__ pixels) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y;
-  if (i >= c.W || j >= c.H) return;
-  const int64_t k = cell_index(c.W, c.H, i, j);
-  if (!(fl[k] & F_FLUID)) {
-    pixels[k] = vis_rgba(80, 80, 80, 255);
-  } else if (enable_pressure && enable_smoke) {
-    const float p = pressure[k];
+// The colour of one cell (update_fluid_pixels_kernel, src/graphics_handler.cu:
+// 262-287, with its three colourings, :214-260); `keep` = the pixel's current
+// value, returned when neither smoke nor pressure colours it.
+__device__ __forceinline__ int pixel_colour(uint32_t flag, float smoke, float p, int keep,
+                                            int enable_pressure, int enable_smoke,
+                                            float min_pressure, float max_pressure) {
+  if (!(flag & F_FLUID)) return vis_rgba(80, 80, 80, 255);
+  if (enable_pressure && enable_smoke) {
     float norm_p = 0;
     if (p < 0 && min_pressure != 0) {
       norm_p = -p / min_pressure;
@@ -69,10 +60,10 @@ __global__ void k_render_pixels(const S* __restrict__ smoke, const float* __rest
     norm_p = vis_clamp(norm_p, -1.0f, 1.0f);
     const float hue = (1.0f - norm_p) * 120.0f;
     uint8_t r, g, b;
-    vis_hsv_to_rgb(hue, 1.0f, ld<float>(smoke + k), r, g, b);
-    pixels[k] = vis_rgba(r, g, b, 255);
-  } else if (enable_pressure) {
-    const float p = pressure[k];
+    vis_hsv_to_rgb(hue, 1.0f, smoke, r, g, b);
+    return vis_rgba(r, g, b, 255);
+  }
+  if (enable_pressure) {
     float norm_p;
     if (p < 0) {
       norm_p = -p / min_pressure;
@@ -83,11 +74,49 @@ __global__ void k_render_pixels(const S* __restrict__ smoke, const float* __rest
     const float hue = (1.0f - norm_p) * 120.0f;
     uint8_t r, g, b;
     vis_hsv_to_rgb(hue, 1.0f, 1.0f, r, g, b);
-    pixels[k] = vis_rgba(r, g, b, 255);
-  } else if (enable_smoke) {
-    const uint8_t col = 255 - static_cast<uint8_t>(ld<float>(smoke + k) * 255);
-    pixels[k] = vis_rgba(255, col, col, 255);
+    return vis_rgba(r, g, b, 255);
   }
+  if (enable_smoke) {
+    const uint8_t col = 255 - static_cast<uint8_t>(smoke * 255);
+    return vis_rgba(255, col, col, 255);
+  }
+  return keep;
+}
+
+// Pixel (x, y) = (i, H - 1 - j) is stored at y * W + x, the cell's own index,
+// so the pass is flat over the W*H cells, four per thread with vector loads
+// and stores where the arrays allow (the pixel buffer 16-byte aligned).
+template <class S>
+__global__ void k_render_pixels(const S* __restrict__ smoke, const float* __restrict__ pressure,
+                                const uint8_t* __restrict__ fl, int64_t n, int enable_pressure,
+                                int enable_smoke, float min_pressure, float max_pressure,
+                                int* __restrict__ pixels, int vec) {
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t k0 = 4 * q;
+  if (k0 >= n) return;
+  if (vec && k0 + 3 < n) {
+    const uint32_t f4 = __ldg(reinterpret_cast<const uint32_t*>(fl + k0));
+    const float4 s4 = enable_smoke ? vec4_to_f32(smoke + k0) : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 p4 = enable_pressure ? __ldg(reinterpret_cast<const float4*>(pressure + k0))
+                                      : make_float4(0.f, 0.f, 0.f, 0.f);
+    int4 keep = make_int4(0, 0, 0, 0);
+    if (!enable_pressure && !enable_smoke) keep = *reinterpret_cast<const int4*>(pixels + k0);
+    int4 out;
+    out.x = pixel_colour(f4 & 0xffu, s4.x, p4.x, keep.x, enable_pressure, enable_smoke,
+                         min_pressure, max_pressure);
+    out.y = pixel_colour((f4 >> 8) & 0xffu, s4.y, p4.y, keep.y, enable_pressure, enable_smoke,
+                         min_pressure, max_pressure);
+    out.z = pixel_colour((f4 >> 16) & 0xffu, s4.z, p4.z, keep.z, enable_pressure, enable_smoke,
+                         min_pressure, max_pressure);
+    out.w = pixel_colour(f4 >> 24, s4.w, p4.w, keep.w, enable_pressure, enable_smoke,
+                         min_pressure, max_pressure);
+    *reinterpret_cast<int4*>(pixels + k0) = out;
+    return;
+  }
+  for (int64_t k = k0; k < n && k < k0 + 4; k++)
+    pixels[k] = pixel_colour(fl[k], enable_smoke ? ld<float>(smoke + k) : 0.0f,
+                             enable_pressure ? pressure[k] : 0.0f, pixels[k], enable_pressure,
+                             enable_smoke, min_pressure, max_pressure);
 }
 
 struct VisualParams {
