@@ -154,7 +154,10 @@ typedef struct os_fields_view {
   int32_t* total_s;   /* Fluid::d_total_s */
   int32_t projection_resident; /* resident forms in use: bit 0 projection,
                                   bit 1 diffusion */
-  int32_t reserved;
+  int32_t tma_staging;   /* 1: diffusion passes stage their regions with tensor
+                            copies (FP32, W and depth multiples of 4; the
+                            environment variable OPENSAYAL_GB300_TMA=0 at
+                            os_create turns it off) */
 } os_fields_view;
 
 typedef struct os_handle os_handle;

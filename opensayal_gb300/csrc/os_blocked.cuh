@@ -25,7 +25,10 @@
 // read as zero (they are never active and never feed an active cell).
 #pragma once
 
+#include <cuda.h>  // CUtensorMap and its enums (types only; no driver-library link)
+
 #include <algorithm>
+#include <mutex>
 #include <type_traits>
 
 namespace osg {
@@ -491,7 +494,10 @@ __device__ __forceinline__ void diff_stage_in(float* A, float* B, int tx, int ty
 
 // `sweeps` Jacobi sweeps on the staged region, A -> B -> A ...; on return A
 // holds the result (the pointers are swapped as the sweeps go). Ends with a
-// barrier.
+// barrier. With FLIP the region's rows are stored top row first (the order
+// of the global layout, as a tensor copy delivers them): region row y sits at
+// row RH - 1 - y.
+template <bool FLIP = false>
 __device__ __forceinline__ void diff_sweeps(float*& A, float*& B, int tx, int ty, const Consts& c,
                                             const StepParams* __restrict__ prm, int sweeps,
                                             int halo, int TX, int TY) {
@@ -517,11 +523,13 @@ __device__ __forceinline__ void diff_sweeps(float*& A, float*& B, int tx, int ty
     const int reach = sweeps - 1 - t;
     const int ya = max(r0, halo - reach), yb = min(r1, RH - halo + reach);
     if (column && x >= halo - reach && x < kRegionW - halo + reach && ya < yb) {
-      float down = A[(ya - 1) * kRegionW + x];
-      float centre = A[ya * kRegionW + x];
+      const int rs = FLIP ? -kRegionW : kRegionW;     // step to the next region row
+      const int base = FLIP ? (RH - 1) * kRegionW : 0;
+      float down = A[base + (ya - 1) * rs + x];
+      float centre = A[base + ya * rs + x];
       for (int y = ya; y < yb; y++) {
-        const int e = y * kRegionW + x;
-        const float up = A[e + kRegionW];
+        const int e = base + y * rs + x;
+        const float up = A[e + rs];
         // src/fluid.cu:178-182: neighbours (i-1, j), (i+1, j), (i, j-1), (i, j+1)
         B[e] = fma_rn(a, A[e - 1] + A[e + 1] + down + up, centre) / fma_rn(4.0f, a, 1.0f);
         down = centre;
@@ -535,19 +543,20 @@ __device__ __forceinline__ void diff_sweeps(float*& A, float*& B, int tx, int ty
   }
 }
 
-// Owned cells of the region in A back to global.
-template <class S>
+// Owned cells of the region in A back to global (FLIP as in diff_sweeps).
+template <class S, bool FLIP = false>
 __device__ __forceinline__ void diff_store_owned(const float* A, int tx, int ty,
                                                  S* __restrict__ u_out, const Consts& c, int halo,
                                                  int TX, int TY) {
   const int gx0 = tx * TX - halo, gy0 = ty * TY - halo;
   const int W = c.W, H = c.H;
+  const int RH = TY + 2 * halo;
   const bool vec = ((W & 3) == 0) && ((gx0 & 3) == 0);
   for (int it = threadIdx.x; it < TY * kQuads; it += blockDim.x) {
     const int y = halo + it / kQuads, x = 4 * (it % kQuads);
     const int i = gx0 + x, j = gy0 + y;
     if (j >= H || i >= W) continue;
-    const float* src = A + y * kRegionW + x;
+    const float* src = A + (FLIP ? RH - 1 - y : y) * kRegionW + x;
     if (vec && x >= halo && x + 3 < halo + TX) {
       store_quad(u_out, W, H, i, j, true, *reinterpret_cast<const float4*>(src));
       continue;
@@ -581,6 +590,98 @@ k_diffuse_blocked(const S* __restrict__ u_in, S* __restrict__ u_out, Consts c,
   extern __shared__ __align__(16) float smem[];
   diffuse_tile<S>(smem, blockIdx.x % tiles_x, blockIdx.x / tiles_x, u_in, u_out, c, prm, sweeps,
                   halo, TX, TY);
+}
+
+// ---------------------------------------------------------------------------
+// Tensor-memory-accelerator staging of the diffusion region (FP32 fields).
+// One thread issues a single 2-D bulk tensor copy of the whole 256 x RH region
+// into A, completing on an mbarrier the block waits on; cells off the grid
+// arrive as zero, as the vector loads stage them. The copy delivers rows in
+// the global (top row first) order, so the sweeps and the write-back run with
+// FLIP. Every wait is bounded: a block whose copy does not complete records
+// the failure in the error words and returns.
+// ---------------------------------------------------------------------------
+constexpr int kTmaSpin = 1 << 22;
+constexpr int kTmaAlign = 128;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+               : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(done)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+
+// The box at (x, row) of `map` into dst; x * 4 bytes must be a multiple of 16.
+__device__ __forceinline__ void tma_load_2d(float* dst, const CUtensorMap* map, int x, int row,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(row), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__global__ void __launch_bounds__(kBlockThreads, 1)
+k_diffuse_blocked_tma(const __grid_constant__ CUtensorMap in_map, float* __restrict__ u_out,
+                      Consts c, const StepParams* __restrict__ prm, int sweeps, int halo, int TX,
+                      int TY, int tiles_x, int* __restrict__ err, int* __restrict__ host_err) {
+  extern __shared__ __align__(16) float smem_tma[];
+  __shared__ __align__(8) uint64_t bar;
+  const int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
+  const int RH = TY + 2 * halo;
+  // Both buffers are copy destinations, 128-byte aligned (the launch adds
+  // room for the alignment and a 128-byte gap between them).
+  float* A = reinterpret_cast<float*>(
+      (reinterpret_cast<uintptr_t>(smem_tma) + kTmaAlign - 1) & ~uintptr_t(kTmaAlign - 1));
+  float* B = A + RH * kRegionW + kTmaAlign / sizeof(float);
+  const int gx0 = tx * TX - halo, gy0 = ty * TY - halo;
+  if (threadIdx.x == 0) mbar_init(&bar, 1);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    // The region into both buffers (cells no sweep updates keep their value
+    // in each), one copy per buffer on the same barrier.
+    mbar_expect_tx(&bar, (uint32_t)(2 * RH * kRegionW * sizeof(float)));
+    tma_load_2d(A, &in_map, gx0, c.H - gy0 - RH, &bar);
+    tma_load_2d(B, &in_map, gx0, c.H - gy0 - RH, &bar);
+  }
+  bool done = false;
+  for (int it = 0; it < kTmaSpin && !done; it++) done = mbar_try_wait(&bar, 0);
+  if (__syncthreads_or(!done)) {
+    if (threadIdx.x == 0) {
+      if (err && atomicCAS(err, 0, 1) == 0 && host_err) {
+        *(volatile int*)host_err = 1;
+        __threadfence_system();
+      }
+      // The copy may still land: give it the same bound again before the
+      // block's shared memory is released.
+      for (int it = 0; it < kTmaSpin && !mbar_try_wait(&bar, 0); it++) {
+      }
+    }
+    __syncthreads();
+    return;
+  }
+  diff_sweeps<true>(A, B, tx, ty, c, prm, sweeps, halo, TX, TY);
+  diff_store_owned<float, true>(A, tx, ty, u_out, c, halo, TX, TY);
 }
 
 // ---------------------------------------------------------------------------
@@ -679,12 +780,81 @@ inline int enqueue_blocked_projection(os_handle* h, cudaStream_t st, int* cur_u,
   return launches;
 }
 
+// Dynamic shared memory of k_diffuse_blocked_tma: two 128-byte aligned
+// buffers of RH x 256 floats and the alignment slack.
+inline size_t tma_diffusion_smem(int RH) {
+  return 2 * (size_t)RH * kRegionW * sizeof(float) + 2 * kTmaAlign;
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library).
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                   const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                   const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+inline EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  });
+  return fn;
+}
+
+// Tensor maps of u and ub (FP32) with a box of one diffusion region, when the
+// copy's rules hold: row pitch and region origin multiples of 16 bytes (W and
+// the halo K multiples of 4), the box at most 256 rows.
+inline bool prepare_tma_diffusion(os_handle* h) {
+  if (h->storage != OS_STORAGE_F32 || h->block_k <= 0 || (h->block_k & 3) || (h->W & 3))
+    return false;
+  const TileGeom g = make_geom(h->W, h->H, h->block_k, false, false, sm_count(h->cfg.device));
+  if (g.RH > 256 || (g.TX & 3) || (g.halo & 3)) return false;
+  if (tma_diffusion_smem(g.RH) + kStaticSmem > kMaxSmem || h->block_k > 8) return false;
+  const EncodeTiledFn enc = encode_tiled();
+  if (!enc) return false;
+  const cuuint64_t dims[2] = {(cuuint64_t)h->W, (cuuint64_t)h->H};
+  const cuuint64_t strides[1] = {(cuuint64_t)h->W * sizeof(float)};
+  const cuuint32_t box[2] = {(cuuint32_t)kRegionW, (cuuint32_t)g.RH};
+  const cuuint32_t elem[2] = {1, 1};
+  for (int k = 0; k < 2; k++) {
+    if (enc(&h->diff_maps[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, k ? h->ub : h->u, dims,
+            strides, box, elem, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return false;
+  }
+  return true;
+}
+
 template <class S>
 inline int enqueue_blocked_diffusion(os_handle* h, cudaStream_t st, int* cur_u) {
   const int K = h->block_k;
   const TileGeom g = make_geom(h->W, h->H, K, false, false, sm_count(h->cfg.device));
   S* U[2] = {static_cast<S*>(h->u), static_cast<S*>(h->ub)};
   const int tiles = g.tiles_x * g.tiles_y;
+  if constexpr (std::is_same<S, float>::value) {
+    if (h->tma_diffusion) {
+      const size_t smem = tma_diffusion_smem(g.RH);
+      cudaFuncSetAttribute(k_diffuse_blocked_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem);
+      int launches = 0;
+      for (int done = 0; done < h->c.n;) {
+        const int sweeps = std::min(K, h->c.n - done);
+        k_diffuse_blocked_tma<<<tiles, kBlockThreads, smem, st>>>(
+            h->diff_maps[*cur_u], U[1 - *cur_u], h->c, h->d_params, sweeps, g.halo, g.TX, g.TY,
+            g.tiles_x, h->rerr, h->d_host_rerr);
+        launches++;
+        *cur_u = 1 - *cur_u;
+        done += sweeps;
+      }
+      return launches;
+    }
+  }
   cudaFuncSetAttribute(k_diffuse_blocked<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)g.smem);
   int launches = 0;

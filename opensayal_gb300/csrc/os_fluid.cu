@@ -9,6 +9,7 @@
 // stream and synchronises, src/fluid.cu:770-795). Per-step inputs (dt and the
 // Source) sit in a device-side StepParams block that is refreshed only when
 // they change, so one graph serves every step.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -159,6 +160,9 @@ struct os_handle {
   double* diag = nullptr;   // diagnostics partials and result (first use)
   // Resident projection (one cooperative launch per phase): tile flags, the
   // device error word, and a mapped host word the kernel sets on a failed wait.
+  // Diffusion passes staged by the tensor memory accelerator: maps of u, ub.
+  CUtensorMap diff_maps[2];
+  bool tma_diffusion = false;
   int resident = 0;       // projection
   int resident_diff = 0;  // diffusion
   unsigned* rflags = nullptr;
@@ -564,6 +568,8 @@ struct TuneChoice {
 };
 TuneChoice autotune_projection(const os_config& base);
 
+int ensure_error_words(os_handle* h);
+
 // Sets up the resident projection (mask bit 0) and diffusion (bit 1) that
 // the grid fits (flags, error words).
 int enable_resident(os_handle* h, int mask) {
@@ -597,13 +603,22 @@ int enable_resident(os_handle* h, int mask) {
   CUDA_OR_RETURN(cudaMemset(h->rflags, 0, fb));
   CUDA_OR_RETURN(cudaMalloc(&h->dflags, fb));
   CUDA_OR_RETURN(cudaMemset(h->dflags, 0, fb));
+  int rc = ensure_error_words(h);
+  if (rc) return rc;
+  h->resident = proj;
+  h->resident_diff = diff;
+  return OS_OK;
+}
+
+// Device error word and the mapped host word a kernel sets on a failed
+// bounded wait (allocated once).
+int ensure_error_words(os_handle* h) {
+  if (h->rerr) return OS_OK;
   CUDA_OR_RETURN(cudaMalloc(&h->rerr, sizeof(int)));
   CUDA_OR_RETURN(cudaMemset(h->rerr, 0, sizeof(int)));
   CUDA_OR_RETURN(cudaHostAlloc(&h->host_rerr, sizeof(int), cudaHostAllocMapped));
   *h->host_rerr = 0;
   CUDA_OR_RETURN(cudaHostGetDevicePointer((void**)&h->d_host_rerr, h->host_rerr, 0));
-  h->resident = proj;
-  h->resident_diff = diff;
   return OS_OK;
 }
 
@@ -614,13 +629,13 @@ int check_resident(os_handle* h) {
   if (!h->host_rerr || *(volatile int*)h->host_rerr == 0) return OS_OK;
   *(volatile int*)h->host_rerr = 0;
   const int sms = sm_count(h->cfg.device);
-  cudaMemsetAsync(h->rflags, 0, (size_t)sms * sizeof(unsigned), h->stream);
-  cudaMemsetAsync(h->dflags, 0, (size_t)sms * sizeof(unsigned), h->stream);
+  if (h->rflags) cudaMemsetAsync(h->rflags, 0, (size_t)sms * sizeof(unsigned), h->stream);
+  if (h->dflags) cudaMemsetAsync(h->dflags, 0, (size_t)sms * sizeof(unsigned), h->stream);
   cudaMemsetAsync(h->rerr, 0, sizeof(int), h->stream);
   cudaStreamSynchronize(h->stream);
   return set_err(OS_ERR_TIMEOUT,
-                 "resident projection or diffusion: a tile gave up waiting for its "
-                 "neighbours; the fields are undefined");
+                 "a bounded device wait gave up (resident projection or diffusion "
+                 "neighbours, or a tensor copy); the fields are undefined");
 }
 
 void free_handle(os_handle* h) {
@@ -859,6 +874,12 @@ static int create_handle(const os_config* cfg, Arena* arena, os_handle** out) {
     const int rc = enable_resident(h, resident);
     if (rc) return fail(rc);
   }
+  const char* tma_env = std::getenv("OPENSAYAL_GB300_TMA");
+  if (!arena && !(tma_env && tma_env[0] == '0') && prepare_tma_diffusion(h)) {
+    const int rc = ensure_error_words(h);
+    if (rc) return fail(rc);
+    h->tma_diffusion = true;
+  }
   *out = h;
   return OS_OK;
 }
@@ -927,6 +948,7 @@ int os_fields(os_handle* h, os_fields_view* out) {
   out->is_solid = h->is_solid;
   out->total_s = h->total_s;
   out->projection_resident = (h->resident ? 1 : 0) | (h->resident_diff ? 2 : 0);
+  out->tma_staging = h->tma_diffusion ? 1 : 0;
   return OS_OK;
 }
 

@@ -103,7 +103,7 @@ class OsFieldsView(C.Structure):
         ("is_solid", C.c_void_p),
         ("total_s", C.c_void_p),
         ("projection_resident", C.c_int32),
-        ("reserved", C.c_int32),
+        ("tma_staging", C.c_int32),
     ]
 
 
