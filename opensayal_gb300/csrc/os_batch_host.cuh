@@ -94,7 +94,7 @@ TileGeom batch_geom(int halo, bool projection, int ty_div = 1) {
 
 size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
 
-void release_member(os_batch* b, os_handle* h) {
+void release_member(os_handle* h) {
   cudaStreamSynchronize(h->stream);
   free_handle(h);
 }
@@ -102,8 +102,8 @@ void release_member(os_batch* b, os_handle* h) {
 void free_batch(os_batch* b) {
   if (!b) return;
   if (b->graph) cudaGraphExecDestroy(b->graph);
-  for (auto& kv : b->members) release_member(b, kv.second.h);
-  for (auto& g : b->graveyard) release_member(b, g.second);
+  for (auto& kv : b->members) release_member(kv.second.h);
+  for (auto& g : b->graveyard) release_member(g.second);
   if (b->d_plan) cudaFree(b->d_plan);
   if (b->d_remaining) cudaFree(b->d_remaining);
   for (int i = 0; i < 2; i++) {
@@ -383,7 +383,7 @@ int batch_progress(os_batch* b) {
   // Cancelled members whose last enqueued steps have completed.
   for (size_t k = 0; k < b->graveyard.size();) {
     if (b->graveyard[k].first <= b->steps_done) {
-      release_member(b, b->graveyard[k].second);
+      release_member(b->graveyard[k].second);
       b->free_slots.push_back(b->graveyard_slots[k]);
       b->graveyard[k] = b->graveyard.back();
       b->graveyard_slots[k] = b->graveyard_slots.back();
@@ -532,12 +532,12 @@ int add_member(os_batch* b, const os_config& cfg, int32_t steps, int64_t* id) {
   int rc = create_handle(&c, b->arena, &h);
   if (rc) return rc;
   if ((rc = push_params(h, nullptr, c.d_t, h->stream))) {
-    release_member(b, h);
+    release_member(h);
     return rc;
   }
   const cudaError_t e = cudaStreamSynchronize(h->stream);
   if (e != cudaSuccess) {
-    release_member(b, h);
+    release_member(h);
     return set_err(OS_ERR_CUDA, "scenario set-up: %s", cudaGetErrorString(e));
   }
   os_batch::Member m;
@@ -619,7 +619,7 @@ int os_batch_remove(os_batch* b, int64_t id) {
   b->members.erase(it);
   if (!m.scheduled || (m.finish_at >= 0 && m.finish_at <= b->steps_done)) {
     // Never stepped, or frozen on the device: nothing in flight touches it.
-    release_member(b, m.h);
+    release_member(m.h);
     b->free_slots.push_back(m.slot);
     return OS_OK;
   }

@@ -451,6 +451,7 @@ k_project_blocked(const S* __restrict__ u_in, const S* __restrict__ v_in,
                   S* __restrict__ u_out, S* __restrict__ v_out, float* __restrict__ p,
                   const uint8_t* __restrict__ fl, Consts c, const StepParams* __restrict__ prm,
                   int sweeps, int halo, int TX, int TY, int tiles_x, int zero_pressure) {
+  pdl_entry();
   extern __shared__ __align__(16) float smem[];
   project_tile<PRESSURE, S>(smem, blockIdx.x % tiles_x, blockIdx.x / tiles_x, u_in, v_in, u_out,
                             v_out, p, fl, c, prm, sweeps, halo, TX, TY, zero_pressure);
@@ -587,6 +588,7 @@ __global__ void __launch_bounds__(kBlockThreads, 1)
 k_diffuse_blocked(const S* __restrict__ u_in, S* __restrict__ u_out, Consts c,
                   const StepParams* __restrict__ prm, int sweeps, int halo, int TX, int TY,
                   int tiles_x) {
+  pdl_entry();
   extern __shared__ __align__(16) float smem[];
   diffuse_tile<S>(smem, blockIdx.x % tiles_x, blockIdx.x / tiles_x, u_in, u_out, c, prm, sweeps,
                   halo, TX, TY);
@@ -645,6 +647,7 @@ __global__ void __launch_bounds__(kBlockThreads, 1)
 k_diffuse_blocked_tma(const __grid_constant__ CUtensorMap in_map, float* __restrict__ u_out,
                       Consts c, const StepParams* __restrict__ prm, int sweeps, int halo, int TX,
                       int TY, int tiles_x, int* __restrict__ err, int* __restrict__ host_err) {
+  pdl_entry();
   extern __shared__ __align__(16) float smem_tma[];
   __shared__ __align__(8) uint64_t bar;
   const int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
@@ -687,6 +690,24 @@ k_diffuse_blocked_tma(const __grid_constant__ CUtensorMap in_map, float* __restr
 // ---------------------------------------------------------------------------
 // Host: tile geometry and pass enqueue.
 // ---------------------------------------------------------------------------
+
+// Launch with programmatic stream serialisation when `pdl` (the kernels call
+// pdl_entry() first, so the dependency on the previous kernel is kept).
+template <class... KArgs, class... Args>
+inline void launch_pdl(bool pdl, void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                       cudaStream_t st, Args&&... args) {
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cfg.attrs = attr;
+  cfg.numAttrs = pdl ? 1 : 0;
+  cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
 
 constexpr size_t kMaxSmem = 227 * 1024;
 constexpr size_t kStaticSmem = 256;
@@ -762,15 +783,16 @@ inline int enqueue_blocked_projection(os_handle* h, cudaStream_t st, int* cur_u,
     if (pressure) {
       cudaFuncSetAttribute(k_project_blocked<true, S>,
                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.smem);
-      k_project_blocked<true, S><<<tiles, kBlockThreads, g.smem, st>>>(
-          uin, vin, uout, vout, h->p, h->flags, h->c, h->d_params, sweeps, g.halo, g.TX, g.TY,
-          g.tiles_x, (zero_first && pass == 0) ? 1 : 0);
+      launch_pdl(h->pdl, k_project_blocked<true, S>, tiles, kBlockThreads, g.smem, st,
+                 uin, vin, uout, vout, h->p, (const uint8_t*)h->flags, h->c,
+                 (const StepParams*)h->d_params, sweeps, g.halo, g.TX, g.TY, g.tiles_x,
+                 (zero_first && pass == 0) ? 1 : 0);
     } else {
       cudaFuncSetAttribute(k_project_blocked<false, S>,
                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.smem);
-      k_project_blocked<false, S><<<tiles, kBlockThreads, g.smem, st>>>(
-          uin, vin, uout, vout, h->p, h->flags, h->c, h->d_params, sweeps, g.halo, g.TX, g.TY,
-          g.tiles_x, 0);
+      launch_pdl(h->pdl, k_project_blocked<false, S>, tiles, kBlockThreads, g.smem, st,
+                 uin, vin, uout, vout, h->p, (const uint8_t*)h->flags, h->c,
+                 (const StepParams*)h->d_params, sweeps, g.halo, g.TX, g.TY, g.tiles_x, 0);
     }
     launches++;
     *cur_u = 1 - *cur_u;
@@ -845,9 +867,9 @@ inline int enqueue_blocked_diffusion(os_handle* h, cudaStream_t st, int* cur_u) 
       int launches = 0;
       for (int done = 0; done < h->c.n;) {
         const int sweeps = std::min(K, h->c.n - done);
-        k_diffuse_blocked_tma<<<tiles, kBlockThreads, smem, st>>>(
-            h->diff_maps[*cur_u], U[1 - *cur_u], h->c, h->d_params, sweeps, g.halo, g.TX, g.TY,
-            g.tiles_x, h->rerr, h->d_host_rerr);
+        launch_pdl(h->pdl, k_diffuse_blocked_tma, tiles, kBlockThreads, smem, st,
+                   h->diff_maps[*cur_u], U[1 - *cur_u], h->c, (const StepParams*)h->d_params,
+                   sweeps, g.halo, g.TX, g.TY, g.tiles_x, h->rerr, h->d_host_rerr);
         launches++;
         *cur_u = 1 - *cur_u;
         done += sweeps;
@@ -860,8 +882,9 @@ inline int enqueue_blocked_diffusion(os_handle* h, cudaStream_t st, int* cur_u) 
   int launches = 0;
   for (int done = 0; done < h->c.n;) {
     const int sweeps = std::min(K, h->c.n - done);
-    k_diffuse_blocked<S><<<tiles, kBlockThreads, g.smem, st>>>(
-        U[*cur_u], U[1 - *cur_u], h->c, h->d_params, sweeps, g.halo, g.TX, g.TY, g.tiles_x);
+    launch_pdl(h->pdl, k_diffuse_blocked<S>, tiles, kBlockThreads, g.smem, st,
+               (const S*)U[*cur_u], U[1 - *cur_u], h->c, (const StepParams*)h->d_params, sweeps,
+               g.halo, g.TX, g.TY, g.tiles_x);
     launches++;
     *cur_u = 1 - *cur_u;
     done += sweeps;

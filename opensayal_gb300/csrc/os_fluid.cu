@@ -163,6 +163,8 @@ struct os_handle {
   // Diffusion passes staged by the tensor memory accelerator: maps of u, ub.
   CUtensorMap diff_maps[2];
   bool tma_diffusion = false;
+  // Step kernels launched with programmatic dependent launch.
+  bool pdl = true;
   int resident = 0;       // projection
   int resident_diff = 0;  // diffusion
   unsigned* rflags = nullptr;
@@ -291,7 +293,7 @@ void enqueue_diffusion(os_handle* h, Vel<S>& w, Enq& q) {
   }
   const dim3 g2((h->W + 127) / 128, h->H);
   for (int t = 0; t < h->c.n; t++) {
-    k_diffuse<S, A><<<g2, 128, 0, q.st>>>(w.U[w.cu], w.U[1 - w.cu], h->c, h->d_params);
+    launch_pdl(h->pdl, k_diffuse<S, A>, g2, 128, 0, q.st, w.U[w.cu], w.U[1 - w.cu], h->c, h->d_params);
     w.cu = 1 - w.cu;
     q.count++;
   }
@@ -316,8 +318,8 @@ void enqueue_projection(os_handle* h, Vel<S>& w, Enq& q, bool zero_pressure_firs
   }
   const dim3 gp(((h->W + 1) / 2 + 127) / 128, h->H);
   for (int t = 0; t < h->c.n; t++) {
-    k_project_half<S, A, 0><<<gp, 128, 0, q.st>>>(w.u(), w.v(), h->p, h->flags, h->c, h->d_params);
-    k_project_half<S, A, 1><<<gp, 128, 0, q.st>>>(w.u(), w.v(), h->p, h->flags, h->c, h->d_params);
+    launch_pdl(h->pdl, k_project_half<S, A, 0>, gp, 128, 0, q.st, w.u(), w.v(), h->p, h->flags, h->c, h->d_params);
+    launch_pdl(h->pdl, k_project_half<S, A, 1>, gp, 128, 0, q.st, w.u(), w.v(), h->p, h->flags, h->c, h->d_params);
     q.count += 2;
   }
 }
@@ -328,12 +330,12 @@ void settle(os_handle* h, Vel<S>& w, Enq& q) {
   const int64_t N = (int64_t)h->N;
   const unsigned g1 = (unsigned)((N + 255) / 256);
   if (w.cu) {
-    k_copy1<S><<<g1, 256, 0, q.st>>>(w.U[1], w.U[0], N);
+    launch_pdl(h->pdl, k_copy1<S>, g1, 256, 0, q.st, w.U[1], w.U[0], N);
     q.count++;
     w.cu = 0;
   }
   if (w.cv) {
-    k_copy1<S><<<g1, 256, 0, q.st>>>(w.V[1], w.V[0], N);
+    launch_pdl(h->pdl, k_copy1<S>, g1, 256, 0, q.st, w.V[1], w.V[0], N);
     q.count++;
     w.cv = 0;
   }
@@ -349,13 +351,13 @@ void enqueue_smoke_advection(os_handle* h, Vel<S>& w, Enq& q) {
   const Consts& c = h->c;
   // smoke advection on the live velocities, copying them back as it goes
   if (w.cu && w.cv)
-    k_advect_smoke<S, A, true, true><<<g2, 128, 0, q.st>>>(w.u(), w.v(), s, sb, u0, v0, h->flags, c, h->d_params);
+    launch_pdl(h->pdl, k_advect_smoke<S, A, true, true>, g2, 128, 0, q.st, w.u(), w.v(), s, sb, u0, v0, h->flags, c, h->d_params);
   else if (w.cu)
-    k_advect_smoke<S, A, true, false><<<g2, 128, 0, q.st>>>(w.u(), w.v(), s, sb, u0, v0, h->flags, c, h->d_params);
+    launch_pdl(h->pdl, k_advect_smoke<S, A, true, false>, g2, 128, 0, q.st, w.u(), w.v(), s, sb, u0, v0, h->flags, c, h->d_params);
   else if (w.cv)
-    k_advect_smoke<S, A, false, true><<<g2, 128, 0, q.st>>>(w.u(), w.v(), s, sb, u0, v0, h->flags, c, h->d_params);
+    launch_pdl(h->pdl, k_advect_smoke<S, A, false, true>, g2, 128, 0, q.st, w.u(), w.v(), s, sb, u0, v0, h->flags, c, h->d_params);
   else
-    k_advect_smoke<S, A, false, false><<<g2, 128, 0, q.st>>>(w.u(), w.v(), s, sb, u0, v0, h->flags, c, h->d_params);
+    launch_pdl(h->pdl, k_advect_smoke<S, A, false, false>, g2, 128, 0, q.st, w.u(), w.v(), s, sb, u0, v0, h->flags, c, h->d_params);
   w.cu = w.cv = 0;
   q.count++;
 }
@@ -373,11 +375,11 @@ int enqueue_phase(os_handle* h, int phase, Enq& q) {
   cudaStream_t st = q.st;
   switch (phase) {
     case OS_PHASE_FORCES:
-      k_forces<S, A><<<g2, 128, 0, st>>>(w.u(), w.v(), s, c, h->smoke_period, h->d_params);
+      launch_pdl(h->pdl, k_forces<S, A>, g2, 128, 0, st, w.u(), w.v(), s, c, h->smoke_period, h->d_params);
       q.count++;
       break;
     case OS_PHASE_ZERO_PRESSURE:
-      k_zero<<<g1, 256, 0, st>>>(h->p, N);
+      launch_pdl(h->pdl, k_zero, g1, 256, 0, st, h->p, N);
       q.count++;
       break;
     case OS_PHASE_DIFFUSION:
@@ -389,27 +391,27 @@ int enqueue_phase(os_handle* h, int phase, Enq& q) {
       settle(h, w, q);
       break;
     case OS_PHASE_PRESSURE_RANGE:
-      k_prange_init<<<1, 32, 0, st>>>(h->d_pkeys);
-      k_prange<<<152 * 4, 256, 0, st>>>(h->p, N, h->d_pkeys);
+      launch_pdl(h->pdl, k_prange_init, 1, 32, 0, st, h->d_pkeys);
+      launch_pdl(h->pdl, k_prange, 152 * 4, 256, 0, st, h->p, N, h->d_pkeys);
       q.count += 2;
       break;
     case OS_PHASE_EXTRAPOLATION:
-      k_extrapolate<S><<<1, 1024, 0, st>>>(w.u(), w.v(), c);
+      launch_pdl(h->pdl, k_extrapolate<S>, 1, 1024, 0, st, w.u(), w.v(), c);
       q.count++;
       break;
     case OS_PHASE_VEL_ADVECTION:
-      k_advect_velocity<S, A><<<g2, 128, 0, st>>>(w.U[0], w.V[0], w.U[1], w.V[1], h->flags, c, h->d_params);
+      launch_pdl(h->pdl, k_advect_velocity<S, A>, g2, 128, 0, st, w.U[0], w.V[0], w.U[1], w.V[1], h->flags, c, h->d_params);
       w.cu = w.cv = 1;
       q.count++;
       settle(h, w, q);
       break;
     case OS_PHASE_SMOKE_ADVECTION:
       enqueue_smoke_advection<S, A>(h, w, q);
-      k_copy1<S><<<g1, 256, 0, st>>>(sb, s, N);
+      launch_pdl(h->pdl, k_copy1<S>, g1, 256, 0, st, sb, s, N);
       q.count++;
       break;
     case OS_PHASE_DECAY:
-      k_finish_smoke<S, A><<<g1, 256, 0, st>>>(s, s, c, h->d_params, N);
+      launch_pdl(h->pdl, k_finish_smoke<S, A>, g1, 256, 0, st, s, s, c, h->d_params, N);
       q.count++;
       break;
     default:
@@ -434,30 +436,30 @@ int enqueue_step(os_handle* h, Enq& q) {
   const dim3 g2((h->W + 127) / 128, h->H);
   const int64_t N = (int64_t)h->N;
   const unsigned g1 = (unsigned)((N + 255) / 256);
-  k_forces<S, A><<<g2, 128, 0, q.st>>>(w.u(), w.v(), s, c, h->smoke_period, h->d_params);
+  launch_pdl(h->pdl, k_forces<S, A>, g2, 128, 0, q.st, w.u(), w.v(), s, c, h->smoke_period, h->d_params);
   q.count++;
   // The blocked projection zeroes the pressure in its first pass.
   if (cfg.enable_pressure && !(use_blocked<S, A>(h) && c.n > 0)) {
-    k_zero<<<g1, 256, 0, q.st>>>(h->p, N);
+    launch_pdl(h->pdl, k_zero, g1, 256, 0, q.st, h->p, N);
     q.count++;
   }
   if (cfg.viscosity != 0.0f) enqueue_diffusion<S, A>(h, w, q);
   enqueue_projection<S, A>(h, w, q, cfg.enable_pressure != 0);
   if (cfg.enable_pressure) {
-    k_prange_init<<<1, 32, 0, q.st>>>(h->d_pkeys);
-    k_prange<<<152 * 4, 256, 0, q.st>>>(h->p, N, h->d_pkeys);
+    launch_pdl(h->pdl, k_prange_init, 1, 32, 0, q.st, h->d_pkeys);
+    launch_pdl(h->pdl, k_prange, 152 * 4, 256, 0, q.st, h->p, N, h->d_pkeys);
     q.count += 2;
   }
-  k_extrapolate<S><<<1, 1024, 0, q.st>>>(w.u(), w.v(), c);
+  launch_pdl(h->pdl, k_extrapolate<S>, 1, 1024, 0, q.st, w.u(), w.v(), c);
   q.count++;
-  k_advect_velocity<S, A><<<g2, 128, 0, q.st>>>(w.u(), w.v(), w.U[1 - w.cu], w.V[1 - w.cv],
+  launch_pdl(h->pdl, k_advect_velocity<S, A>, g2, 128, 0, q.st, w.u(), w.v(), w.U[1 - w.cu], w.V[1 - w.cv],
                                                  h->flags, c, h->d_params);
   w.cu = 1 - w.cu;
   w.cv = 1 - w.cv;
   q.count++;
   if (cfg.enable_smoke && cfg.tunnel_smoke != 0.0f) {
     enqueue_smoke_advection<S, A>(h, w, q);
-    k_finish_smoke<S, A><<<g1, 256, 0, q.st>>>(sb, s, c, h->d_params, N);
+    launch_pdl(h->pdl, k_finish_smoke<S, A>, g1, 256, 0, q.st, sb, s, c, h->d_params, N);
     q.count++;
   } else {
     settle(h, w, q);
@@ -874,6 +876,8 @@ static int create_handle(const os_config* cfg, Arena* arena, os_handle** out) {
     const int rc = enable_resident(h, resident);
     if (rc) return fail(rc);
   }
+  const char* pdl_env = std::getenv("OPENSAYAL_GB300_PDL");
+  h->pdl = !(pdl_env && pdl_env[0] == '0');
   const char* tma_env = std::getenv("OPENSAYAL_GB300_TMA");
   if (!arena && !(tma_env && tma_env[0] == '0') && prepare_tma_diffusion(h)) {
     const int rc = ensure_error_words(h);

@@ -153,7 +153,8 @@ class Server:
             state, left = b.status(mid)
             rep.cell_steps += req.cells * (req.steps - max(left, 0))
         rep.wall_s = clock() - t0
-        rep.arrived += len(pending)
+        # Requests that arrived before the end but were never taken up.
+        rep.arrived += sum(1 for r in pending if r.arrival < rep.wall_s)
         return rep
 
 
