@@ -155,9 +155,9 @@ typedef struct os_fields_view {
   int32_t projection_resident; /* resident forms in use: bit 0 projection,
                                   bit 1 diffusion */
   int32_t tma_staging;   /* 1: diffusion passes stage their regions with tensor
-                            copies (FP32, W and depth multiples of 4; the
-                            environment variable OPENSAYAL_GB300_TMA=0 at
-                            os_create turns it off) */
+                            copies; opt-in with the environment variable
+                            OPENSAYAL_GB300_TMA=1 at os_create (FP32, W and
+                            depth multiples of 4, depth at most 8) */
 } os_fields_view;
 
 typedef struct os_handle os_handle;

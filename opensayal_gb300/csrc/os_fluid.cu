@@ -878,8 +878,11 @@ static int create_handle(const os_config* cfg, Arena* arena, os_handle** out) {
   }
   const char* pdl_env = std::getenv("OPENSAYAL_GB300_PDL");
   h->pdl = !(pdl_env && pdl_env[0] == '0');
+  // Tensor-copy staging of the diffusion passes is opt-in: inside a step it
+  // measured 2% slower than the vector loads (with programmatic launch both
+  // overlap the previous kernel, the vector loads more so).
   const char* tma_env = std::getenv("OPENSAYAL_GB300_TMA");
-  if (!arena && !(tma_env && tma_env[0] == '0') && prepare_tma_diffusion(h)) {
+  if (!arena && tma_env && tma_env[0] == '1' && prepare_tma_diffusion(h)) {
     const int rc = ensure_error_words(h);
     if (rc) return fail(rc);
     h->tma_diffusion = true;
