@@ -341,23 +341,41 @@ void settle(os_handle* h, Vel<S>& w, Enq& q) {
   }
 }
 
+// Advection launches: the unit cell size (sim.cell_size 1, the default) has
+// its own instantiation, in which the divisions by the cell size fold away.
+template <class S, class A>
+void launch_velocity_advection(os_handle* h, cudaStream_t st, S* u, S* v, S* ub, S* vb) {
+  const dim3 g2((h->W + 127) / 128, h->H);
+  if (h->c.h == 1)
+    launch_pdl(h->pdl, k_advect_velocity<S, A, 1>, g2, 128, 0, st, u, v, ub, vb, h->flags, h->c, h->d_params);
+  else
+    launch_pdl(h->pdl, k_advect_velocity<S, A, 0>, g2, 128, 0, st, u, v, ub, vb, h->flags, h->c, h->d_params);
+}
+
+template <class S, class A, bool COPY_U, bool COPY_V>
+void launch_smoke_advection(os_handle* h, cudaStream_t st, S* ub, S* vb, S* s, S* sb, S* u0, S* v0) {
+  const dim3 g2((h->W + 127) / 128, h->H);
+  if (h->c.h == 1)
+    launch_pdl(h->pdl, k_advect_smoke<S, A, COPY_U, COPY_V, 1>, g2, 128, 0, st, ub, vb, s, sb, u0, v0, h->flags, h->c, h->d_params);
+  else
+    launch_pdl(h->pdl, k_advect_smoke<S, A, COPY_U, COPY_V, 0>, g2, 128, 0, st, ub, vb, s, sb, u0, v0, h->flags, h->c, h->d_params);
+}
+
 template <class S, class A>
 void enqueue_smoke_advection(os_handle* h, Vel<S>& w, Enq& q) {
   S* s = static_cast<S*>(h->s);
   S* sb = static_cast<S*>(h->sb);
   S* u0 = w.U[0];
   S* v0 = w.V[0];
-  const dim3 g2((h->W + 127) / 128, h->H);
-  const Consts& c = h->c;
   // smoke advection on the live velocities, copying them back as it goes
   if (w.cu && w.cv)
-    launch_pdl(h->pdl, k_advect_smoke<S, A, true, true>, g2, 128, 0, q.st, w.u(), w.v(), s, sb, u0, v0, h->flags, c, h->d_params);
+    launch_smoke_advection<S, A, true, true>(h, q.st, w.u(), w.v(), s, sb, u0, v0);
   else if (w.cu)
-    launch_pdl(h->pdl, k_advect_smoke<S, A, true, false>, g2, 128, 0, q.st, w.u(), w.v(), s, sb, u0, v0, h->flags, c, h->d_params);
+    launch_smoke_advection<S, A, true, false>(h, q.st, w.u(), w.v(), s, sb, u0, v0);
   else if (w.cv)
-    launch_pdl(h->pdl, k_advect_smoke<S, A, false, true>, g2, 128, 0, q.st, w.u(), w.v(), s, sb, u0, v0, h->flags, c, h->d_params);
+    launch_smoke_advection<S, A, false, true>(h, q.st, w.u(), w.v(), s, sb, u0, v0);
   else
-    launch_pdl(h->pdl, k_advect_smoke<S, A, false, false>, g2, 128, 0, q.st, w.u(), w.v(), s, sb, u0, v0, h->flags, c, h->d_params);
+    launch_smoke_advection<S, A, false, false>(h, q.st, w.u(), w.v(), s, sb, u0, v0);
   w.cu = w.cv = 0;
   q.count++;
 }
@@ -368,14 +386,12 @@ int enqueue_phase(os_handle* h, int phase, Enq& q) {
   Vel<S> w = vel_of<S>(h);
   S* s = static_cast<S*>(h->s);
   S* sb = static_cast<S*>(h->sb);
-  const int W = h->W, H = h->H;
   const int64_t N = (int64_t)h->N;
-  const dim3 g2((W + 127) / 128, H);
   const unsigned g1 = (unsigned)((N + 255) / 256);
   cudaStream_t st = q.st;
   switch (phase) {
     case OS_PHASE_FORCES:
-      launch_pdl(h->pdl, k_forces<S, A>, g2, 128, 0, st, w.u(), w.v(), s, c, h->smoke_period, h->d_params);
+      launch_pdl(h->pdl, k_forces<S, A>, cell_grid(h->W, h->H), kCellThreads, 0, st, w.u(), w.v(), s, c, h->smoke_period, h->d_params);
       q.count++;
       break;
     case OS_PHASE_ZERO_PRESSURE:
@@ -400,7 +416,7 @@ int enqueue_phase(os_handle* h, int phase, Enq& q) {
       q.count++;
       break;
     case OS_PHASE_VEL_ADVECTION:
-      launch_pdl(h->pdl, k_advect_velocity<S, A>, g2, 128, 0, st, w.U[0], w.V[0], w.U[1], w.V[1], h->flags, c, h->d_params);
+      launch_velocity_advection<S, A>(h, st, w.U[0], w.V[0], w.U[1], w.V[1]);
       w.cu = w.cv = 1;
       q.count++;
       settle(h, w, q);
@@ -411,7 +427,7 @@ int enqueue_phase(os_handle* h, int phase, Enq& q) {
       q.count++;
       break;
     case OS_PHASE_DECAY:
-      launch_pdl(h->pdl, k_finish_smoke<S, A>, g1, 256, 0, st, s, s, c, h->d_params, N);
+      launch_pdl(h->pdl, k_finish_smoke<S, A>, (unsigned)((h->N + 256 * kCellsPerThread - 1) / (256 * kCellsPerThread)), 256, 0, st, s, s, c, h->d_params, N);
       q.count++;
       break;
     default:
@@ -433,10 +449,9 @@ int enqueue_step(os_handle* h, Enq& q) {
   S* s = static_cast<S*>(h->s);
   S* sb = static_cast<S*>(h->sb);
   const Consts& c = h->c;
-  const dim3 g2((h->W + 127) / 128, h->H);
   const int64_t N = (int64_t)h->N;
   const unsigned g1 = (unsigned)((N + 255) / 256);
-  launch_pdl(h->pdl, k_forces<S, A>, g2, 128, 0, q.st, w.u(), w.v(), s, c, h->smoke_period, h->d_params);
+  launch_pdl(h->pdl, k_forces<S, A>, cell_grid(h->W, h->H), kCellThreads, 0, q.st, w.u(), w.v(), s, c, h->smoke_period, h->d_params);
   q.count++;
   // The blocked projection zeroes the pressure in its first pass.
   if (cfg.enable_pressure && !(use_blocked<S, A>(h) && c.n > 0)) {
@@ -452,14 +467,13 @@ int enqueue_step(os_handle* h, Enq& q) {
   }
   launch_pdl(h->pdl, k_extrapolate<S>, 1, 1024, 0, q.st, w.u(), w.v(), c);
   q.count++;
-  launch_pdl(h->pdl, k_advect_velocity<S, A>, g2, 128, 0, q.st, w.u(), w.v(), w.U[1 - w.cu], w.V[1 - w.cv],
-                                                 h->flags, c, h->d_params);
+  launch_velocity_advection<S, A>(h, q.st, w.u(), w.v(), w.U[1 - w.cu], w.V[1 - w.cv]);
   w.cu = 1 - w.cu;
   w.cv = 1 - w.cv;
   q.count++;
   if (cfg.enable_smoke && cfg.tunnel_smoke != 0.0f) {
     enqueue_smoke_advection<S, A>(h, w, q);
-    launch_pdl(h->pdl, k_finish_smoke<S, A>, g1, 256, 0, q.st, sb, s, c, h->d_params, N);
+    launch_pdl(h->pdl, k_finish_smoke<S, A>, (unsigned)((h->N + 256 * kCellsPerThread - 1) / (256 * kCellsPerThread)), 256, 0, q.st, sb, s, c, h->d_params, N);
     q.count++;
   } else {
     settle(h, w, q);
