@@ -198,7 +198,7 @@ k_batch_project(const PlanHeader* __restrict__ P, const int* __restrict__ remain
                               nullptr, d.flags, d.c, halo, TX, TY, 0);
     });
     __syncthreads();
-    proj_sweeps<false>(smem, d.c, d.prm, sweeps, halo, TY);
+    proj_sweeps_fast<false>(smem, d.c, d.prm, sweeps, halo, TY);
     with_storage(d.storage, [&](auto tag) {
       using S = std::remove_pointer_t<decltype(tag)>;
       proj_stage_out<false, S>(smem, tx, ty, copy_of<S>(d.u, d.ub, 1 - iu),

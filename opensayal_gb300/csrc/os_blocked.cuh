@@ -390,6 +390,216 @@ __device__ __forceinline__ void proj_sweeps(float* smem, const Consts& c,
   }
 }
 
+// ---------------------------------------------------------------------------
+// The same sweeps with the vertical faces in registers.
+//
+// Thread t owns the column pair (2p, 2p + 1), p = t % 128, over the R rows
+// [y0, y0 + R) of strip s = t / 128, y0 = s * R. R is even, so every strip
+// starts on an even row and the active column of the pair in row y0 + r is
+// (r + colour) & 1 for every thread: fixed once the row loop is unrolled. The
+// thread's faces v(x, y0 .. y0 + R - 1) stay in registers for all the sweeps of
+// a pass (one load from and one store to the v planes per pass); only u, the
+// flags and p are read and written in shared memory, and lanes take
+// consecutive words, so there are no bank conflicts. Per cell update that is
+// 2 loads and 2 stores of u and a flag byte, against 4 face loads, 4 face
+// stores and the flags when all faces live in shared memory.
+//
+// The face v(x, Y) on the boundary Y = y0 + R between a strip and the one
+// above belongs to a cell of each: both keep a copy. A half-sweep changes at
+// most one of the two copies of each such face (the lower strip's where its
+// top-row cell is active, the upper strip's where its bottom-row cell is), and
+// that side then writes the new value to the face's own word in the v plane;
+// after the barrier the other side reads it. The word is next written by the
+// side that just read it, so one barrier per half-sweep suffices.
+// ---------------------------------------------------------------------------
+// project_faces without branches, for cells taken two rows at a time: `f` is
+// the flag byte of an active cell and 0 for any cell not updated (inactive,
+// off the cone or off the region), whose faces then keep their values. The
+// expressions are project_faces' own.
+template <bool PRESSURE>
+__device__ __forceinline__ void project_faces_sel(uint32_t f, const Consts& c, float d_t,
+                                                  float& uc, float& right_u, float& vc,
+                                                  float& top_v, float& pc) {
+  const float divergence = right_u - uc + top_v - vc;
+  const int sn = __popc(f & F_NBR_MASK);
+  const float velocity_diff = mul_rn(c.o, divergence / (float)sn);
+  if (PRESSURE) {
+    const float np = pc + velocity_diff * c.density * (float)c.h / d_t;
+    pc = f ? np : pc;
+  }
+  uc = (f & F_LEFT) ? uc + velocity_diff : uc;
+  right_u = (f & F_RIGHT) ? right_u - velocity_diff : right_u;
+  vc = (f & F_BOTTOM) ? vc + velocity_diff : vc;
+  top_v = (f & F_TOP) ? top_v - velocity_diff : top_v;
+}
+
+// One row of a half-sweep, with branches (the accumulated pressure needs the
+// registers that the paired, branch-free rows below would use): the active
+// cell in column CC of row r.
+template <int CC, bool PRESSURE, int R>
+__device__ __forceinline__ void vreg_row(const ProjPlanes& P, float (&v)[2][R], float (&vt)[2],
+                                         int p, int y0, int r, bool in, const Consts& c,
+                                         float d_t) {
+  if (!in) return;
+  const int e = (y0 + r) * kHalfW + p;
+  const uint32_t f = (CC ? P.fo : P.fe)[e];
+  if (!(f & F_ACTIVE)) return;
+  float* uL = (CC ? P.uo : P.ue) + e;
+  float* uR = CC ? P.ue + e + 1 : P.uo + e;
+  float a0 = *uL, a1 = *uR, pp = 0.0f;
+  if (PRESSURE) pp = (CC ? P.po : P.pe)[e];
+  float& top = (r + 1 < R) ? v[CC][r + 1] : vt[CC];
+  project_faces<PRESSURE>(f, c, d_t, a0, a1, v[CC][r], top, pp);
+  *uL = a0;
+  *uR = a1;
+  if (PRESSURE) (CC ? P.po : P.pe)[e] = pp;
+}
+
+// One colour half-sweep over the thread's strip. Rows go two at a time (the
+// two active cells sit in different columns and share no face): both rows'
+// loads first, then both updates, then both stores, with no branches, so the
+// two dependency chains overlap. A pair of rows wholly outside the cone or
+// the region is skipped (a branch that is the same for the whole warp); a
+// single such row, or a column off the cone, is predicated off. An inactive
+// cell in the cone stores its faces unchanged (no other cell of the colour
+// touches them).
+template <int COLOUR, bool PRESSURE, int R>
+__device__ __forceinline__ void vreg_half_sweep(const ProjPlanes& P, float (&v)[2][R],
+                                                float (&vt)[2], int p, int y0, int RH, int halo,
+                                                int reach, const Consts& c, float d_t) {
+  const int lo = max(0, halo - 1 - reach);      // first needed cell, both axes
+  const int y_end = min(RH - 1, RH - halo + reach);
+  const int x_end = kRegionW - halo + reach;    // at most 255: u(x + 1) stays in the row
+  const int rlo = min(max(lo - y0, 0), R), rhi = min(max(y_end - y0, 0), R);
+  const uint32_t rows = ((1u << rhi) - 1u) & ~((1u << rlo) - 1u);
+  const bool col_ok[2] = {2 * p >= lo && 2 * p < x_end, 2 * p + 1 >= lo && 2 * p + 1 < x_end};
+  constexpr int ca = COLOUR & 1, cb = ca ^ 1;   // active columns of even and odd rows
+#pragma unroll
+  for (int r = 0; r < R; r += 2) {
+    if (((rows >> r) & 3u) == 0u) continue;  // both rows off the cone: the same for the warp
+    const bool ia = ((rows >> r) & 1u) && col_ok[ca];
+    const bool ib = ((rows >> (r + 1)) & 1u) && col_ok[cb];
+    if constexpr (PRESSURE) {
+      vreg_row<ca, PRESSURE, R>(P, v, vt, p, y0, r, ia, c, d_t);
+      vreg_row<cb, PRESSURE, R>(P, v, vt, p, y0, r + 1, ib, c, d_t);
+      continue;
+    }
+    const int ea = (y0 + r) * kHalfW + p, eb = ea + kHalfW;
+    float* uLa = (ca ? P.uo : P.ue) + ea;
+    float* uRa = ca ? P.ue + ea + 1 : P.uo + ea;
+    float* uLb = (cb ? P.uo : P.ue) + eb;
+    float* uRb = cb ? P.ue + eb + 1 : P.uo + eb;
+    uint32_t fa = ia ? (ca ? P.fo : P.fe)[ea] : 0u;
+    uint32_t fb = ib ? (cb ? P.fo : P.fe)[eb] : 0u;
+    float a0 = ia ? *uLa : 0.0f, a1 = ia ? *uRa : 0.0f;
+    float b0 = ib ? *uLb : 0.0f, b1 = ib ? *uRb : 0.0f;
+    float pa = 0.0f, pb = 0.0f;
+    if (PRESSURE) {
+      pa = ia ? (ca ? P.po : P.pe)[ea] : 0.0f;
+      pb = ib ? (cb ? P.po : P.pe)[eb] : 0.0f;
+    }
+    fa = (fa & F_ACTIVE) ? fa : 0u;
+    fb = (fb & F_ACTIVE) ? fb : 0u;
+    float& top_b = (r + 2 < R) ? v[cb][r + 2] : vt[cb];
+    project_faces_sel<PRESSURE>(fa, c, d_t, a0, a1, v[ca][r], v[ca][r + 1], pa);
+    project_faces_sel<PRESSURE>(fb, c, d_t, b0, b1, v[cb][r + 1], top_b, pb);
+    if (ia) {
+      *uLa = a0;
+      *uRa = a1;
+      if (PRESSURE) (ca ? P.po : P.pe)[ea] = pa;
+    }
+    if (ib) {
+      *uLb = b0;
+      *uRb = b1;
+      if (PRESSURE) (cb ? P.po : P.pe)[eb] = pb;
+    }
+  }
+  // Boundary faces this half-sweep may have changed, for the neighbouring strip.
+  const int cT = (R - 1 + COLOUR) & 1;  // active column of the top row
+  const int cB = COLOUR & 1;            // active column of the bottom row
+  if (y0 + R < RH) (cT ? P.vo : P.ve)[(y0 + R) * kHalfW + p] = vt[cT];
+  if (y0 > 0 && y0 < RH) (cB ? P.vo : P.ve)[y0 * kHalfW + p] = v[cB][0];
+}
+
+// After the barrier that ends a half-sweep: the neighbours' changed copies.
+template <int COLOUR, int R>
+__device__ __forceinline__ void vreg_receive(const ProjPlanes& P, float (&v)[2][R], float (&vt)[2],
+                                             int p, int y0, int RH) {
+  const int cT = (R - 1 + COLOUR) & 1;
+  const int cB = COLOUR & 1;
+  if (y0 + R < RH) vt[cB] = (cB ? P.vo : P.ve)[(y0 + R) * kHalfW + p];
+  if (y0 > 0 && y0 < RH) v[cT][0] = (cT ? P.vo : P.ve)[y0 * kHalfW + p];
+}
+
+// `sweeps` red/black sweeps on the staged tile (RH <= R * blockDim.x / 128),
+// whose planes start at the base of the dynamic shared memory; the v planes
+// hold the result on return. Ends with a barrier. Not inlined: every storage
+// type's kernels call the one copy (the constants come by value).
+template <bool PRESSURE, int R>
+__device__ __noinline__ void proj_sweeps_vreg(const Consts c, float d_t, int sweeps, int halo,
+                                              int TY) {
+  static_assert(R % 2 == 0, "strips must start on even rows");
+  extern __shared__ __align__(16) float dyn_smem[];
+  const int RH = TY + 2 * halo;
+  const ProjPlanes P = proj_planes<PRESSURE>(dyn_smem, RH);
+  const int p = threadIdx.x % kHalfW;
+  const int y0 = (threadIdx.x / kHalfW) * R;
+  float v[2][R], vt[2];
+#pragma unroll
+  for (int r = 0; r < R; r++) {
+    const int e = (y0 + r) * kHalfW + p;
+    const bool in = y0 + r < RH;
+    v[0][r] = in ? P.ve[e] : 0.0f;
+    v[1][r] = in ? P.vo[e] : 0.0f;
+  }
+  const bool top_in = y0 + R < RH;
+  vt[0] = top_in ? P.ve[(y0 + R) * kHalfW + p] : 0.0f;
+  vt[1] = top_in ? P.vo[(y0 + R) * kHalfW + p] : 0.0f;
+  // Every thread has its copies before any boundary word is rewritten.
+  __syncthreads();
+  for (int t = 0; t < sweeps; t++) {
+    const int reach = 2 * (sweeps - t) - 1;  // half-sweeps after the even one
+    vreg_half_sweep<0, PRESSURE, R>(P, v, vt, p, y0, RH, halo, reach, c, d_t);
+    __syncthreads();
+    vreg_receive<0, R>(P, v, vt, p, y0, RH);
+    vreg_half_sweep<1, PRESSURE, R>(P, v, vt, p, y0, RH, halo, reach - 1, c, d_t);
+    __syncthreads();
+    vreg_receive<1, R>(P, v, vt, p, y0, RH);
+  }
+#pragma unroll
+  for (int r = 0; r < R; r++) {
+    const int e = (y0 + r) * kHalfW + p;
+    if (y0 + r < RH) {
+      P.ve[e] = v[0][r];
+      P.vo[e] = v[1][r];
+    }
+  }
+  __syncthreads();
+}
+
+// The sweeps with registers where the region's rows fit the strips, else
+// with every face in shared memory. `smem` is the dynamic shared memory base.
+template <bool PRESSURE>
+__device__ __forceinline__ void proj_sweeps_fast(float* smem, const Consts& c,
+                                                 const StepParams* __restrict__ prm, int sweeps,
+                                                 int halo, int TY) {
+  const int RH = TY + 2 * halo;
+  const int strips = blockDim.x / kHalfW;
+  const float d_t = prm->dt;
+  if (RH <= 8 * strips)
+    proj_sweeps_vreg<PRESSURE, 8>(c, d_t, sweeps, halo, TY);
+  else if (RH <= 10 * strips)
+    proj_sweeps_vreg<PRESSURE, 10>(c, d_t, sweeps, halo, TY);
+  else if (RH <= 12 * strips)
+    proj_sweeps_vreg<PRESSURE, 12>(c, d_t, sweeps, halo, TY);
+  else if (RH <= 14 * strips)
+    proj_sweeps_vreg<PRESSURE, 14>(c, d_t, sweeps, halo, TY);
+  else if (RH <= 16 * strips)
+    proj_sweeps_vreg<PRESSURE, 16>(c, d_t, sweeps, halo, TY);
+  else
+    proj_sweeps<PRESSURE>(smem, c, prm, sweeps, halo, TY);
+}
+
 // Owned cells back out; halo and TX are multiples of 4 when `vec` holds.
 template <bool PRESSURE, class S>
 __device__ __forceinline__ void proj_stage_out(float* smem, int tx, int ty, S* __restrict__ u_out,
@@ -441,7 +651,7 @@ __device__ __forceinline__ void project_tile(float* smem, int tx, int ty,
                                              int halo, int TX, int TY, int zero_pressure) {
   proj_stage_in<PRESSURE, S>(smem, tx, ty, u_in, v_in, p, fl, c, halo, TX, TY, zero_pressure);
   __syncthreads();
-  proj_sweeps<PRESSURE>(smem, c, prm, sweeps, halo, TY);
+  proj_sweeps_fast<PRESSURE>(smem, c, prm, sweeps, halo, TY);
   proj_stage_out<PRESSURE, S>(smem, tx, ty, u_out, v_out, p, c, halo, TX, TY);
 }
 

@@ -216,7 +216,7 @@ k_project_resident(S* U0, S* U1, S* V0, S* V1, int cu, int cv, float* __restrict
   const int passes = (c.n + K - 1) / K;
   const int hq = halo / 4, oq0 = hq, oq1 = hq + TX / 4;  // owned quads
   for (int q = 0; q < passes; q++) {
-    proj_sweeps<PRESSURE>(smem, c, prm, min(K, c.n - q * K), halo, TY);
+    proj_sweeps_fast<PRESSURE>(smem, c, prm, min(K, c.n - q * K), halo, TY);
     S* uo = ((cu + q + 1) & 1) ? U1 : U0;
     S* vo = ((cv + q + 1) & 1) ? V1 : V0;
     if (q == passes - 1) {
