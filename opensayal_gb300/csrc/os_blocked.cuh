@@ -600,6 +600,56 @@ __device__ __forceinline__ void proj_sweeps_fast(float* smem, const Consts& c,
     proj_sweeps<PRESSURE>(smem, c, prm, sweeps, halo, TY);
 }
 
+// apply_extrapolation_at (src/fluid.cu:720-733) on the owned cells of a
+// staged region, in extrapolate_grid's order: the row rules for every owned
+// column, then the column rules for every owned row. Each rule reads a cell of
+// the tile that writes it as long as the last tile row and column hold at
+// least two cells, which the caller checks; the grid's rules then need no
+// other tile. Ends with a barrier.
+template <bool PRESSURE>
+__device__ __forceinline__ void extrapolate_region(float* smem, int RH, int gx0, int gy0,
+                                                   int halo, int TX, int TY, int W, int H) {
+  const ProjPlanes P = proj_planes<PRESSURE>(smem, RH);
+  const int i0 = gx0 + halo, i1 = min(gx0 + halo + TX, W);  // owned global columns
+  const int j0 = gy0 + halo, j1 = min(gy0 + halo + TY, H);  // owned global rows
+  auto U = [&](int i, int j) -> float& {
+    const int x = i - gx0;
+    return ((x & 1) ? P.uo : P.ue)[(j - gy0) * kHalfW + (x >> 1)];
+  };
+  auto V = [&](int i, int j) -> float& {
+    const int x = i - gx0;
+    return ((x & 1) ? P.vo : P.ve)[(j - gy0) * kHalfW + (x >> 1)];
+  };
+  const bool bottom = j0 == 0, top = j1 == H;
+  if (bottom || top) {
+    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+      if (bottom) {
+        U(i, 0) = U(i, 1);
+        V(i, 1) = 0.0f;
+      }
+      if (top) U(i, H - 1) = U(i, H - 2);
+    }
+  }
+  __syncthreads();
+  const bool left = i0 == 0, right = i1 == W;
+  if (left || right) {
+    for (int j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
+      if (left) {
+        V(0, j) = V(1, j);
+        U(1, j) = 0.0f;
+      }
+      if (right) V(W - 1, j) = V(W - 2, j);
+    }
+  }
+  __syncthreads();
+}
+
+// Whether extrapolate_region can stand for the extrapolation kernel on this
+// tile grid: the last tile row and column hold at least two cells each.
+inline bool extrapolation_tile_local(int W, int H, int TX, int TY) {
+  return W >= 3 && H >= 3 && TX >= 2 && TY >= 2 && (W - 1) % TX != 0 && (H - 1) % TY != 0;
+}
+
 // Owned cells back out; halo and TX are multiples of 4 when `vec` holds.
 template <bool PRESSURE, class S>
 __device__ __forceinline__ void proj_stage_out(float* smem, int tx, int ty, S* __restrict__ u_out,

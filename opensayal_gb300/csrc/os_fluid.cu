@@ -299,11 +299,17 @@ void enqueue_diffusion(os_handle* h, Vel<S>& w, Enq& q) {
   }
 }
 
+// With `extrapolated` non-null, the resident form may apply the extrapolation
+// that follows in a step to its last pass's regions; *extrapolated says
+// whether it did.
 template <class S, class A>
-void enqueue_projection(os_handle* h, Vel<S>& w, Enq& q, bool zero_pressure_first) {
+void enqueue_projection(os_handle* h, Vel<S>& w, Enq& q, bool zero_pressure_first,
+                        bool* extrapolated = nullptr) {
+  if (extrapolated) *extrapolated = false;
   if constexpr (kBlockedTypes<S, A>) {
     if (use_blocked<S, A>(h) && h->resident) {
-      const int n = enqueue_resident_projection<S>(h, q.st, &w.cu, &w.cv, zero_pressure_first);
+      const int n = enqueue_resident_projection<S>(h, q.st, &w.cu, &w.cv, zero_pressure_first,
+                                                   extrapolated);
       if (n > 0) {
         q.count += n;
         return;
@@ -459,14 +465,17 @@ int enqueue_step(os_handle* h, Enq& q) {
     q.count++;
   }
   if (cfg.viscosity != 0.0f) enqueue_diffusion<S, A>(h, w, q);
-  enqueue_projection<S, A>(h, w, q, cfg.enable_pressure != 0);
+  bool extrapolated = false;
+  enqueue_projection<S, A>(h, w, q, cfg.enable_pressure != 0, &extrapolated);
   if (cfg.enable_pressure) {
     launch_pdl(h->pdl, k_prange_init, 1, 32, 0, q.st, h->d_pkeys);
     launch_pdl(h->pdl, k_prange, 152 * 4, 256, 0, q.st, h->p, N, h->d_pkeys);
     q.count += 2;
   }
-  launch_pdl(h->pdl, k_extrapolate<S>, 1, 1024, 0, q.st, w.u(), w.v(), c);
-  q.count++;
+  if (!extrapolated) {
+    launch_pdl(h->pdl, k_extrapolate<S>, 1, 1024, 0, q.st, w.u(), w.v(), c);
+    q.count++;
+  }
   launch_velocity_advection<S, A>(h, q.st, w.u(), w.v(), w.U[1 - w.cu], w.V[1 - w.cv]);
   w.cu = 1 - w.cu;
   w.cv = 1 - w.cv;

@@ -201,7 +201,7 @@ __global__ void __launch_bounds__(kBlockThreads, 1)
 k_project_resident(S* U0, S* U1, S* V0, S* V1, int cu, int cv, float* __restrict__ p,
                    const uint8_t* __restrict__ fl, Consts c, const StepParams* __restrict__ prm,
                    int K, int halo, int TX, int TY, int tiles_x, int tiles_y, ResidentSync sync,
-                   int zero_pressure) {
+                   int zero_pressure, int extrapolate) {
   extern __shared__ __align__(16) float smem[];
   const int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
   const int RH = TY + 2 * halo;
@@ -220,6 +220,7 @@ k_project_resident(S* U0, S* U1, S* V0, S* V1, int cu, int cv, float* __restrict
     S* uo = ((cu + q + 1) & 1) ? U1 : U0;
     S* vo = ((cv + q + 1) & 1) ? V1 : V0;
     if (q == passes - 1) {
+      if (extrapolate) extrapolate_region<PRESSURE>(smem, RH, gx0, gy0, halo, TX, TY, W, H);
       proj_stage_out<PRESSURE, S>(smem, tx, ty, uo, vo, p, c, halo, TX, TY);
       return;
     }
@@ -454,11 +455,15 @@ inline bool resident_launchable(const TileGeom& g, int sms) {
 // advance as after ceil(n/K) passes of the pass engine.
 template <class S>
 inline int enqueue_resident_projection(os_handle* h, cudaStream_t st, int* cur_u, int* cur_v,
-                                       bool zero_first) {
+                                       bool zero_first, bool* extrapolated) {
   const int K = h->block_k;
   const bool pressure = h->cfg.enable_pressure != 0;
   TileGeom g;
   if (!resident_geom(h->W, h->H, K, pressure, sm_count(h->cfg.device), &g)) return -1;
+  // The extrapolation that follows the projection in a step, on the staged
+  // regions of the last pass.
+  const int extrapolate =
+      (extrapolated && h->c.n > 0 && extrapolation_tile_local(h->W, h->H, g.TX, g.TY)) ? 1 : 0;
   S* U0 = static_cast<S*>(h->u);
   S* U1 = static_cast<S*>(h->ub);
   S* V0 = static_cast<S*>(h->v);
@@ -481,16 +486,17 @@ inline int enqueue_resident_projection(os_handle* h, cudaStream_t st, int* cur_u
     e = cudaLaunchKernelEx(&cfg, k_project_resident<true, S>, U0, U1, V0, V1, *cur_u, *cur_v,
                            h->p, (const uint8_t*)h->flags, h->c,
                            (const StepParams*)h->d_params, K, g.halo, g.TX, g.TY, g.tiles_x,
-                           g.tiles_y, rs, zero_first ? 1 : 0);
+                           g.tiles_y, rs, zero_first ? 1 : 0, extrapolate);
   } else {
     cudaFuncSetAttribute(k_project_resident<false, S>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.smem);
     e = cudaLaunchKernelEx(&cfg, k_project_resident<false, S>, U0, U1, V0, V1, *cur_u, *cur_v,
                            h->p, (const uint8_t*)h->flags, h->c,
                            (const StepParams*)h->d_params, K, g.halo, g.TX, g.TY, g.tiles_x,
-                           g.tiles_y, rs, 0);
+                           g.tiles_y, rs, 0, extrapolate);
   }
   if (e != cudaSuccess) return -1;
+  if (extrapolated) *extrapolated = extrapolate != 0;
   const int passes = (h->c.n + K - 1) / K;
   if (passes & 1) {
     *cur_u = 1 - *cur_u;
