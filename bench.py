@@ -235,6 +235,8 @@ def run_gb300(args, world, rank, local) -> dict | None:
         cfg.projection_block = args.block
     if args.resident is not None:
         cfg.projection_resident = args.resident
+    if args.diffusion_block is not None:
+        cfg.diffusion_block = args.diffusion_block
     cells = cfg.width * cfg.height
     f = Fluid(cfg)
     u, v = scenarios.perturbation(2, f.download("is_solid"))
@@ -320,6 +322,7 @@ def run_gb300(args, world, rank, local) -> dict | None:
                           "achieved": step_bytes * value / world / 1e9, "unit": "GB/s",
                           "frac": step_bytes * value / world / 1e9 / pk["hbm_gbs"]},
         "phase_ms": {"projection": proj_ms / 3, "diffusion": diff_ms / 3},
+        "phase_launches": {"projection": proj_kernels // 3, "diffusion": diff_kernels // 3},
         "wall_s": wall,
         "clocks": clk.summary(),
     }
@@ -623,6 +626,9 @@ def main():
     ap.add_argument("--scenarios", type=int, default=512, help="batched workload size")
     ap.add_argument("--block", type=int, default=None,
                     help="red/black sweeps per blocked pass (0 autotune, -1 plain)")
+    ap.add_argument("--diffusion-block", type=int, default=None,
+                    help="Jacobi sweeps per diffusion pass (0: the projection's depth or, "
+                         "autotuned, the autotuner's)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--resident", type=int, default=None, choices=[-1, 0, 1, 2, 3],
                     help="phases as resident cooperative launches: mask 1 projection, "

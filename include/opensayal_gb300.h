@@ -128,7 +128,13 @@ typedef struct os_config {
                                diffusion: a multiple of 4); 0 = the autotuner
                                decides (with projection_block 0; a fixed
                                projection_block runs pass by pass); -1 = never */
-  int32_t reserved[3];
+  int32_t diffusion_block; /* Jacobi sweeps fused per diffusion pass when the
+                               diffusion runs pass by pass (not resident):
+                               0 = projection_block's depth, or with
+                               projection_block 0 the autotuner's choice
+                               (its halo is K cells against the projection's
+                               2K, so deeper passes can pay) */
+  int32_t reserved[2];
 } os_config;
 
 /* The reference's `Source` (inc/fluid.cuh:8-13), the interactive forcing. */

@@ -1003,6 +1003,9 @@ inline int choose_block_k(const os_handle* h) {
   return 0;
 }
 
+// Jacobi sweeps per blocked diffusion pass.
+inline int diffusion_depth(const os_handle* h) { return h->diff_k > 0 ? h->diff_k : h->block_k; }
+
 // FP32 arithmetic on FP32, FP16 or BF16 storage. With reduced storage a value
 // is rounded to storage once per pass (the region stays FP32 in shared
 // memory), not once per sweep as in the plain kernels.
@@ -1093,11 +1096,11 @@ inline EncodeTiledFn encode_tiled() {
 // copy's rules hold: row pitch and region origin multiples of 16 bytes (W and
 // the halo K multiples of 4), the box at most 256 rows.
 inline bool prepare_tma_diffusion(os_handle* h) {
-  if (h->storage != OS_STORAGE_F32 || h->block_k <= 0 || (h->block_k & 3) || (h->W & 3))
-    return false;
-  const TileGeom g = make_geom(h->W, h->H, h->block_k, false, false, sm_count(h->cfg.device));
+  const int K = diffusion_depth(h);
+  if (h->storage != OS_STORAGE_F32 || K <= 0 || (K & 3) || (h->W & 3)) return false;
+  const TileGeom g = make_geom(h->W, h->H, K, false, false, sm_count(h->cfg.device));
   if (g.RH > 256 || (g.TX & 3) || (g.halo & 3)) return false;
-  if (tma_diffusion_smem(g.RH) + kStaticSmem > kMaxSmem || h->block_k > 8) return false;
+  if (tma_diffusion_smem(g.RH) + kStaticSmem > kMaxSmem || K > 8) return false;
   const EncodeTiledFn enc = encode_tiled();
   if (!enc) return false;
   const cuuint64_t dims[2] = {(cuuint64_t)h->W, (cuuint64_t)h->H};
@@ -1115,7 +1118,7 @@ inline bool prepare_tma_diffusion(os_handle* h) {
 
 template <class S>
 inline int enqueue_blocked_diffusion(os_handle* h, cudaStream_t st, int* cur_u) {
-  const int K = h->block_k;
+  const int K = diffusion_depth(h);
   const TileGeom g = make_geom(h->W, h->H, K, false, false, sm_count(h->cfg.device));
   S* U[2] = {static_cast<S*>(h->u), static_cast<S*>(h->ub)};
   const int tiles = g.tiles_x * g.tiles_y;

@@ -141,6 +141,7 @@ struct os_handle {
   size_t esize = 4;
   int smoke_period = 1;
   int block_k = 0;  // red/black sweeps per blocked pass; -1: plain form
+  int diff_k = 0;   // Jacobi sweeps per blocked diffusion pass; 0: block_k
   cudaStream_t stream = nullptr;
   // fields (reference layout); u, v, s in storage precision
   void *u = nullptr, *v = nullptr, *s = nullptr;
@@ -576,6 +577,7 @@ int validate(const os_config* c) {
   if (c->idw_mode < 0 || c->idw_mode > 2) return set_err(OS_ERR_INVALID, "idw_mode must be 0, 1 or 2");
   if (c->projection_resident < -1 || c->projection_resident > 3)
     return set_err(OS_ERR_INVALID, "projection_resident must be -1, 0, 1, 2 or 3");
+  if (c->diffusion_block < 0) return set_err(OS_ERR_INVALID, "diffusion_block must be >= 0");
   if (c->smoke_count != 1) {
     if (c->smoke_count - 1 == 0) return set_err(OS_ERR_INVALID, "smoke_count");
     const int spacing = (c->pipe_height - c->smoke_count * c->smoke_height) / (c->smoke_count - 1);
@@ -586,10 +588,12 @@ int validate(const os_config* c) {
   return OS_OK;
 }
 
-// Blocking depth and projection form chosen by timing, per configuration shape.
+// Blocking depth and projection form chosen by timing, per configuration
+// shape, and the diffusion's own pass depth where it runs pass by pass.
 struct TuneChoice {
   int K;
   int resident;
+  int diff_k;  // 0: K
 };
 TuneChoice autotune_projection(const os_config& base);
 
@@ -829,6 +833,7 @@ static int create_handle(const os_config* cfg, Arena* arena, os_handle** out) {
     h->smoke_period = spacing + cfg->smoke_height;
   }
   h->block_k = choose_block_k(h);
+  h->diff_k = cfg->diffusion_block > 0 ? std::min(cfg->diffusion_block, 32) : 0;
 
   auto fail = [&](int code) {
     free_handle(h);
@@ -892,6 +897,7 @@ static int create_handle(const os_config* cfg, Arena* arena, os_handle** out) {
     } else {
       const TuneChoice t = autotune_projection(*cfg);
       h->block_k = t.K;
+      if (t.diff_k > 0) h->diff_k = t.diff_k;
       resident = t.resident;
     }
   }
@@ -1319,10 +1325,11 @@ int os_profile_phase(os_handle* h, int32_t phase, const os_source* src, float dt
 namespace {
 
 struct TuneKey {
-  int W, H, n, viscous, pressure, storage, device, resident;
+  int W, H, n, viscous, pressure, storage, device, resident, diffusion_block;
   bool operator<(const TuneKey& o) const {
-    return std::tie(W, H, n, viscous, pressure, storage, device, resident) <
-           std::tie(o.W, o.H, o.n, o.viscous, o.pressure, o.storage, o.device, o.resident);
+    return std::tie(W, H, n, viscous, pressure, storage, device, resident, diffusion_block) <
+           std::tie(o.W, o.H, o.n, o.viscous, o.pressure, o.storage, o.device, o.resident,
+                    o.diffusion_block);
   }
 };
 std::map<TuneKey, TuneChoice> g_tuned;
@@ -1352,13 +1359,13 @@ float time_steps(os_handle* t, float dt, int warm, int reps) {
 // the grid fits them; a positive projection_resident fixes the forms and
 // leaves only the depth to choose.
 TuneChoice autotune_projection(const os_config& base) {
-  constexpr TuneChoice kDefault{4, 0};
+  constexpr TuneChoice kDefault{4, 0, 0};
   const char* env = std::getenv("OPENSAYAL_GB300_AUTOTUNE");
   if (env && env[0] == '0')
-    return TuneChoice{kDefault.K, base.projection_resident > 0 ? base.projection_resident : 0};
+    return TuneChoice{kDefault.K, base.projection_resident > 0 ? base.projection_resident : 0, 0};
   const TuneKey key{base.width, base.height, base.projection_n, base.viscosity != 0.0f,
                     base.enable_pressure != 0, base.storage, base.device,
-                    base.projection_resident};
+                    base.projection_resident, base.diffusion_block};
   {
     std::lock_guard<std::mutex> lock(g_tune_mu);
     auto it = g_tuned.find(key);
@@ -1367,38 +1374,48 @@ TuneChoice autotune_projection(const os_config& base) {
   std::vector<TuneChoice> cands;
   for (int K : {2, 4, 6, 8, 12}) {
     if (base.projection_resident > 0) {
-      cands.push_back({K, base.projection_resident});
+      cands.push_back({K, base.projection_resident, 0});
       continue;
     }
-    cands.push_back({K, 0});
+    cands.push_back({K, 0, 0});
     if (base.projection_resident == -1) continue;
-    if (K % 2 == 0 && K <= 8) cands.push_back({K, 1});
+    if (K % 2 == 0 && K <= 8) cands.push_back({K, 1, 0});
     if (K % 4 == 0 && base.viscosity != 0.0f) {
-      cands.push_back({K, 2});
-      if (K <= 8) cands.push_back({K, 3});
+      cands.push_back({K, 2, 0});
+      if (K <= 8) cands.push_back({K, 3, 0});
     }
   }
   const float dt = base.d_t > 0.0f ? base.d_t : 0.05f;
   TuneChoice best = kDefault;
   float best_ms = 0.0f;
-  for (const TuneChoice& cand : cands) {
-    if (cand.K > std::max(1, base.projection_n)) continue;
+  auto try_choice = [&](const TuneChoice& cand) {
     os_config c = base;
     c.projection_block = cand.K;
     c.projection_resident = cand.resident ? cand.resident : -1;
     os_handle* t = nullptr;
-    if (os_create(&c, &t) != OS_OK) continue;  // e.g. out of memory: skip
+    if (os_create(&c, &t) != OS_OK) return;  // e.g. out of memory: skip
     const int got = (t->resident ? 1 : 0) | (t->resident_diff ? 2 : 0);
     if (got != cand.resident) {  // the grid does not fit that form
       os_destroy(t);
-      continue;
+      return;
     }
+    if (cand.diff_k > 0) t->diff_k = cand.diff_k;  // before the first step captures the graph
     const float ms = time_steps(t, dt, 3, 12);
     os_destroy(t);
     if (ms > 0.0f && (best_ms == 0.0f || ms < best_ms)) {
       best_ms = ms;
       best = cand;
     }
+  };
+  for (const TuneChoice& cand : cands)
+    if (cand.K <= std::max(1, base.projection_n)) try_choice(cand);
+  // Deeper diffusion passes than the projection's (the Jacobi halo is half
+  // the red/black one), when the diffusion runs pass by pass.
+  if (base.viscosity != 0.0f && base.diffusion_block == 0 && best_ms > 0.0f &&
+      !(best.resident & 2)) {
+    const TuneChoice chosen = best;
+    for (int dk : {12, 16, 20})
+      if (dk > chosen.K && dk <= base.projection_n) try_choice({chosen.K, chosen.resident, dk});
   }
   g_err[0] = '\0';  // a candidate that failed is not the caller's error
   std::lock_guard<std::mutex> lock(g_tune_mu);

@@ -66,7 +66,8 @@ class OsConfig(C.Structure):
         ("projection_block", C.c_int32),
         ("idw_mode", C.c_int32),
         ("projection_resident", C.c_int32),
-        ("reserved", C.c_int32 * 3),
+        ("diffusion_block", C.c_int32),
+        ("reserved", C.c_int32 * 2),
     ]
 
     def copy(self) -> "OsConfig":

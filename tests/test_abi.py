@@ -127,7 +127,7 @@ def test_load_config_dotted_and_nested_keys(lib_built):
 @pytest.mark.parametrize("bad", [
     dict(width=2), dict(height=1), dict(cell_size=0.5), dict(projection_n=-1),
     dict(storage=9), dict(smoke_count=2, pipe_height=10, smoke_height=10),
-    dict(block_size_x=0),
+    dict(block_size_x=0), dict(projection_resident=4), dict(diffusion_block=-2),
 ])
 def test_invalid_configs_are_rejected_before_any_device_work(lib_built, bad):
     lib = native.load()

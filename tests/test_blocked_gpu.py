@@ -81,3 +81,52 @@ def test_default_workload_blocked_equals_plain(gpu):
         b.update(None, cfg.d_t)
     for field in FIELDS:
         assert same_bits(a.download(field), b.download(field)), field
+
+
+@pytest.mark.parametrize("w,h", [(1920, 1080), (300, 77), (17, 9)])
+@pytest.mark.parametrize("k,dk", [(8, 16), (4, 12), (8, 20), (2, 32)])
+def test_diffusion_depth_apart_from_projection(gpu, w, h, k, dk):
+    """diffusion_block sets the Jacobi sweeps per diffusion pass apart from
+    the projection's depth; the results stay those of the plain kernels."""
+    base = tunnel(w, h, viscosity=0.02, projection_n=37)
+    solid = oracle.OracleFluid(base).is_solid
+    state = random_state(base, 33, solid)
+    plain_cfg = base.copy()
+    plain_cfg.projection_block = -1
+    blocked_cfg = base.copy()
+    blocked_cfg.projection_block = k
+    blocked_cfg.diffusion_block = dk
+    blocked_cfg.projection_resident = -1
+    a, b = load_lib(plain_cfg, state), load_lib(blocked_cfg, state)
+    a.run_phase(native.PHASE_DIFFUSION, None, 0.05)
+    b.run_phase(native.PHASE_DIFFUSION, None, 0.05)
+    ms, launches = b.profile_phase(native.PHASE_DIFFUSION, None, 0.05, 1)
+    # ceil(37 / dk) passes, plus a copy back when their count is odd
+    passes = -(-37 // dk)
+    assert launches == passes + (passes % 2)
+    b.run_phase(native.PHASE_DIFFUSION, None, 0.05)
+    a.run_phase(native.PHASE_DIFFUSION, None, 0.05)
+    a.run_phase(native.PHASE_DIFFUSION, None, 0.05)
+    for field in FIELDS:
+        x, y = a.download(field), b.download(field)
+        assert same_bits(x, y), f"{field}: {int((x != y).sum())} cells differ"
+    a.close()
+    b.close()
+
+
+def test_diffusion_depth_in_steps_with_resident_projection(gpu):
+    cfg = scenarios.default_tunnel_config()
+    state = perturbed_state(cfg, 5)
+    plain_cfg = cfg.copy()
+    plain_cfg.projection_block = -1
+    deep = cfg.copy()
+    deep.projection_block = 8
+    deep.projection_resident = 1
+    deep.diffusion_block = 16
+    a, b = load_lib(plain_cfg, state), load_lib(deep, state)
+    assert b.fields().projection_resident == 1
+    for _ in range(3):
+        a.update(None, cfg.d_t)
+        b.update(None, cfg.d_t)
+    for field in FIELDS:
+        assert same_bits(a.download(field), b.download(field)), field
