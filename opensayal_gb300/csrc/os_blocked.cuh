@@ -207,18 +207,34 @@ __device__ __forceinline__ ProjPlanes proj_planes(float* smem, int RH) {
 // steps through rows 2*(blockDim/128) apart, so its parity, and with it every
 // plane offset, is fixed for the whole loop. Planes are addressed as word
 // offsets from the __shared__ base: ue 0, uo 1, ve 2, vo 3, pe 4, po 5 (x plane).
+// A cell's flag byte as the blocked sweeps keep it in shared memory: 0 for a
+// cell the projection does not update (not F_ACTIVE); otherwise bit 0 set, the
+// neighbour bits F_LEFT .. F_TOP in place, and in bits 5-7 the number of
+// fluid neighbours, s of apply_projection_at (0 to 4). The per-cell test and
+// count are then one compare and one shift.
+constexpr int kSweepCountShift = 5;
+__device__ __forceinline__ uint32_t sweep_flag(uint32_t f) {
+  return (f & F_ACTIVE) ? 1u | (f & F_NBR_MASK) |
+                              ((uint32_t)__popc(f & F_NBR_MASK) << kSweepCountShift)
+                        : 0u;
+}
+__device__ __forceinline__ uint32_t sweep_flags4(uint32_t q) {
+  return sweep_flag(q & 0xffu) | sweep_flag((q >> 8) & 0xffu) << 8 |
+         sweep_flag((q >> 16) & 0xffu) << 16 | sweep_flag(q >> 24) << 24;
+}
+
 // apply_projection_at (src/fluid.cu:229-262) for one cell given its four faces
-// and flag byte; faces it may not touch come back unchanged. (A table of the
-// reciprocals of s in shared memory gives the same bits as the fast-math
+// and sweep flag byte; faces it may not touch come back unchanged. (A table of
+// the reciprocals of s in shared memory gives the same bits as the fast-math
 // division, but measured slower: shared-memory traffic, not the reciprocal,
 // binds these sweeps.)
 template <bool PRESSURE>
 __device__ __forceinline__ void project_faces(uint32_t f, const Consts& c, float d_t, float& uc,
                                               float& right_u, float& vc, float& top_v,
                                               float& pc) {
-  if (!(f & F_ACTIVE)) return;
+  if (!f) return;
   const float divergence = right_u - uc + top_v - vc;
-  const int sn = __popc(f & F_NBR_MASK);
+  const int sn = (int)(f >> kSweepCountShift);
   // A rounded product: the reference keeps it (its later use sits behind a
   // runtime branch) rather than fusing it into the four face updates.
   const float velocity_diff = mul_rn(c.o, divergence / (float)sn);
@@ -250,7 +266,7 @@ __device__ __forceinline__ void proj_rows(float* __restrict__ S, const uint8_t* 
   for (int y = y_begin; y < y_end; y += rows_per_iter) {
     const int s = y * kHalfW + k;
     const uint32_t f2 = *reinterpret_cast<const uint16_t*>(F + oF + s);
-    if (!(f2 & (F_ACTIVE | (F_ACTIVE << 8)))) continue;
+    if (!f2) continue;
     float2 uL = *reinterpret_cast<const float2*>(S + oL + s);
     float2 vB = *reinterpret_cast<const float2*>(S + oV + s);
     float2 vT = *reinterpret_cast<const float2*>(S + oV + s + kHalfW);
@@ -353,7 +369,7 @@ __device__ __forceinline__ void proj_stage_in(float* smem, int tx, int ty,
       *reinterpret_cast<float2*>(P.uo + s) = make_float2(uq[r].y, uq[r].w);
       *reinterpret_cast<float2*>(P.ve + s) = make_float2(vq[r].x, vq[r].z);
       *reinterpret_cast<float2*>(P.vo + s) = make_float2(vq[r].y, vq[r].w);
-      const uint32_t f = fq[r];
+      const uint32_t f = sweep_flags4(fq[r]);
       *reinterpret_cast<uint16_t*>(P.fe + s) = (uint16_t)((f & 0xffu) | ((f >> 8) & 0xff00u));
       *reinterpret_cast<uint16_t*>(P.fo + s) = (uint16_t)(((f >> 8) & 0xffu) | ((f >> 16) & 0xff00u));
     }
@@ -413,15 +429,15 @@ __device__ __forceinline__ void proj_sweeps(float* smem, const Consts& c,
 // side that just read it, so one barrier per half-sweep suffices.
 // ---------------------------------------------------------------------------
 // project_faces without branches, for cells taken two rows at a time: `f` is
-// the flag byte of an active cell and 0 for any cell not updated (inactive,
-// off the cone or off the region), whose faces then keep their values. The
-// expressions are project_faces' own.
+// the sweep flag byte, 0 for any cell not updated (inactive, off the cone or
+// off the region), whose faces then keep their values. The expressions are
+// project_faces' own.
 template <bool PRESSURE>
 __device__ __forceinline__ void project_faces_sel(uint32_t f, const Consts& c, float d_t,
                                                   float& uc, float& right_u, float& vc,
                                                   float& top_v, float& pc) {
   const float divergence = right_u - uc + top_v - vc;
-  const int sn = __popc(f & F_NBR_MASK);
+  const int sn = (int)(f >> kSweepCountShift);
   const float velocity_diff = mul_rn(c.o, divergence / (float)sn);
   if (PRESSURE) {
     const float np = pc + velocity_diff * c.density * (float)c.h / d_t;
@@ -443,7 +459,7 @@ __device__ __forceinline__ void vreg_row(const ProjPlanes& P, float (&v)[2][R], 
   if (!in) return;
   const int e = (y0 + r) * kHalfW + p;
   const uint32_t f = (CC ? P.fo : P.fe)[e];
-  if (!(f & F_ACTIVE)) return;
+  if (!f) return;
   float* uL = (CC ? P.uo : P.ue) + e;
   float* uR = CC ? P.ue + e + 1 : P.uo + e;
   float a0 = *uL, a1 = *uR, pp = 0.0f;
@@ -489,8 +505,8 @@ __device__ __forceinline__ void vreg_half_sweep(const ProjPlanes& P, float (&v)[
     float* uRa = ca ? P.ue + ea + 1 : P.uo + ea;
     float* uLb = (cb ? P.uo : P.ue) + eb;
     float* uRb = cb ? P.ue + eb + 1 : P.uo + eb;
-    uint32_t fa = ia ? (ca ? P.fo : P.fe)[ea] : 0u;
-    uint32_t fb = ib ? (cb ? P.fo : P.fe)[eb] : 0u;
+    const uint32_t fa = ia ? (ca ? P.fo : P.fe)[ea] : 0u;
+    const uint32_t fb = ib ? (cb ? P.fo : P.fe)[eb] : 0u;
     float a0 = ia ? *uLa : 0.0f, a1 = ia ? *uRa : 0.0f;
     float b0 = ib ? *uLb : 0.0f, b1 = ib ? *uRb : 0.0f;
     float pa = 0.0f, pb = 0.0f;
@@ -498,8 +514,6 @@ __device__ __forceinline__ void vreg_half_sweep(const ProjPlanes& P, float (&v)[
       pa = ia ? (ca ? P.po : P.pe)[ea] : 0.0f;
       pb = ib ? (cb ? P.po : P.pe)[eb] : 0.0f;
     }
-    fa = (fa & F_ACTIVE) ? fa : 0u;
-    fb = (fb & F_ACTIVE) ? fb : 0u;
     float& top_b = (r + 2 < R) ? v[cb][r + 2] : vt[cb];
     project_faces_sel<PRESSURE>(fa, c, d_t, a0, a1, v[ca][r], v[ca][r + 1], pa);
     project_faces_sel<PRESSURE>(fb, c, d_t, b0, b1, v[cb][r + 1], top_b, pb);
