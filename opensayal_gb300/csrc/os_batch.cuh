@@ -43,6 +43,7 @@ struct ScenarioDesc {
   const StepParams* prm;
   void *u, *v, *ub, *vb, *s, *sb;
   const uint8_t* flags;
+  const uint16_t* nbr;  // fluid neighbourhoods (samplers)
 };
 
 struct TileRef {
@@ -234,7 +235,7 @@ __global__ void k_batch_advect_velocity(const PlanHeader* __restrict__ P,
       for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x)
         advect_velocity_cell<S, float>(copy_of<S>(d.u, d.ub, iu), copy_of<S>(d.v, d.vb, iv),
                                        copy_of<S>(d.u, d.ub, 1 - iu),
-                                       copy_of<S>(d.v, d.vb, 1 - iv), d.flags, d.c, d.prm, i, j);
+                                       copy_of<S>(d.v, d.vb, 1 - iv), d.nbr, d.c, d.prm, i, j);
     });
   });
 }
@@ -254,7 +255,7 @@ __global__ void k_batch_advect_smoke(const PlanHeader* __restrict__ P,
       for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
         if (d.smoke_on) {
           advect_smoke_cell<S, float>(lu, lv, static_cast<S*>(d.s), static_cast<S*>(d.sb), u, v,
-                                      d.flags, d.c, d.prm, i, j, iu == 1, iv == 1);
+                                      d.nbr, d.c, d.prm, i, j, iu == 1, iv == 1);
         } else {
           const int64_t q = cell_index(d.c.W, d.c.H, i, j);
           if (iu) u[q] = lu[q];

@@ -184,6 +184,7 @@ ScenarioDesc describe(const os_batch* b, const os_handle* h) {
   d.s = h->s;
   d.sb = h->sb;
   d.flags = h->flags;
+  d.nbr = h->nbr;
   return d;
 }
 

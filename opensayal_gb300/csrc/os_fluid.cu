@@ -149,6 +149,7 @@ struct os_handle {
   float* p = nullptr;
   int32_t *is_solid = nullptr, *total_s = nullptr;
   uint8_t* flags = nullptr;
+  uint16_t* nbr = nullptr;  // fluid neighbourhoods of [-1, W] x [-1, H] (samplers)
   StepParams* d_params = nullptr;
   StepParams* h_params = nullptr;        // pinned staging slot
   cudaEvent_t params_event = nullptr;    // completion of the last copy out of it
@@ -190,13 +191,14 @@ namespace {
 constexpr size_t kDiagBytes = (256 + 1) * 7 * sizeof(double);
 
 // Device bytes a handle of this configuration takes from an arena: fields and
-// their buffers, pressure, mask, counts, flags, the parameter block, the
-// pressure keys and, for 16-bit storage, the FP32 transfer staging.
+// their buffers, pressure, mask, counts, flags, neighbourhoods, the parameter
+// block, the pressure keys and, for 16-bit storage, the FP32 transfer staging.
 size_t handle_footprint(const os_config& c) {
   const size_t N = (size_t)c.width * c.height;
   const size_t e = storage_bytes(c.storage);
   auto r = [](size_t b) { return (b + 255) / 256 * 256; };
   size_t bytes = 6 * r(N * e) + 3 * r(N * 4) + r(N) + r(sizeof(StepParams)) + r(2 * sizeof(int));
+  bytes += r((size_t)(c.width + 2) * (c.height + 2) * sizeof(uint16_t));
   if (c.storage != OS_STORAGE_F32) bytes += r(N * 4);
   bytes += r(kDiagBytes);
   return bytes;
@@ -354,18 +356,18 @@ template <class S, class A>
 void launch_velocity_advection(os_handle* h, cudaStream_t st, S* u, S* v, S* ub, S* vb) {
   const dim3 g2((h->W + 127) / 128, h->H);
   if (h->c.h == 1)
-    launch_pdl(h->pdl, k_advect_velocity<S, A, 1>, g2, 128, 0, st, u, v, ub, vb, h->flags, h->c, h->d_params);
+    launch_pdl(h->pdl, k_advect_velocity<S, A, 1>, g2, 128, 0, st, u, v, ub, vb, h->nbr, h->c, h->d_params);
   else
-    launch_pdl(h->pdl, k_advect_velocity<S, A, 0>, g2, 128, 0, st, u, v, ub, vb, h->flags, h->c, h->d_params);
+    launch_pdl(h->pdl, k_advect_velocity<S, A, 0>, g2, 128, 0, st, u, v, ub, vb, h->nbr, h->c, h->d_params);
 }
 
 template <class S, class A, bool COPY_U, bool COPY_V>
 void launch_smoke_advection(os_handle* h, cudaStream_t st, S* ub, S* vb, S* s, S* sb, S* u0, S* v0) {
   const dim3 g2((h->W + 127) / 128, h->H);
   if (h->c.h == 1)
-    launch_pdl(h->pdl, k_advect_smoke<S, A, COPY_U, COPY_V, 1>, g2, 128, 0, st, ub, vb, s, sb, u0, v0, h->flags, h->c, h->d_params);
+    launch_pdl(h->pdl, k_advect_smoke<S, A, COPY_U, COPY_V, 1>, g2, 128, 0, st, ub, vb, s, sb, u0, v0, h->nbr, h->c, h->d_params);
   else
-    launch_pdl(h->pdl, k_advect_smoke<S, A, COPY_U, COPY_V, 0>, g2, 128, 0, st, ub, vb, s, sb, u0, v0, h->flags, h->c, h->d_params);
+    launch_pdl(h->pdl, k_advect_smoke<S, A, COPY_U, COPY_V, 0>, g2, 128, 0, st, ub, vb, s, sb, u0, v0, h->nbr, h->c, h->d_params);
 }
 
 template <class S, class A>
@@ -671,7 +673,7 @@ void free_handle(os_handle* h) {
   if (!h) return;
   if (h->graph) cudaGraphExecDestroy(h->graph);
   void* ptrs[] = {h->u, h->v, h->s, h->ub, h->vb, h->sb, h->p, h->is_solid,
-                  h->total_s, h->flags, h->d_params, h->d_pkeys, h->conv, h->diag};
+                  h->total_s, h->flags, h->nbr, h->d_params, h->d_pkeys, h->conv, h->diag};
   for (void* q : ptrs) dev_free(h, q);
   if (h->arena_block) h->arena->release(h->arena_block);
   if (h->h_pkeys) cudaFreeHost(h->h_pkeys);
@@ -864,6 +866,8 @@ static int create_handle(const os_config* cfg, Arena* arena, os_handle** out) {
       (e = dev_alloc(h, (void**)&h->is_solid, h->N * 4)) != cudaSuccess ||
       (e = dev_alloc(h, (void**)&h->total_s, h->N * 4)) != cudaSuccess ||
       (e = dev_alloc(h, (void**)&h->flags, h->N)) != cudaSuccess ||
+      (e = dev_alloc(h, (void**)&h->nbr, (size_t)(h->W + 2) * (h->H + 2) * sizeof(uint16_t))) !=
+          cudaSuccess ||
       (e = dev_alloc(h, (void**)&h->d_params, sizeof(StepParams))) != cudaSuccess ||
       (e = dev_alloc(h, (void**)&h->d_pkeys, 2 * sizeof(int))) != cudaSuccess)
     return fail(set_err(OS_ERR_NOMEM, "cudaMalloc: %s", cudaGetErrorString(e)));
@@ -886,7 +890,9 @@ static int create_handle(const os_config* cfg, Arena* arena, os_handle** out) {
   const dim3 g2((h->W + 127) / 128, h->H);
   k_init_solid<<<g2, 128, 0, h->stream>>>(h->is_solid, c, m);
   k_init_flags<<<g2, 128, 0, h->stream>>>(h->is_solid, h->total_s, h->flags, c);
-  h->launches += 2;
+  k_init_neighbourhoods<<<dim3((h->W + 2 + 127) / 128, h->H + 2), 128, 0, h->stream>>>(
+      h->is_solid, h->nbr, c);
+  h->launches += 3;
   if ((e = cudaGetLastError()) != cudaSuccess ||
       (e = cudaStreamSynchronize(h->stream)) != cudaSuccess)
     return fail(set_err(OS_ERR_CUDA, "init: %s", cudaGetErrorString(e)));
@@ -1167,15 +1173,15 @@ int os_render_arrows(os_handle* h, const os_visual_config* v, os_arrow* d_arrows
   switch (h->storage) {
     case OS_STORAGE_F32:
       k_render_arrows<float><<<g, b, 0, st>>>((const float*)h->u, (const float*)h->v, h->flags,
-                                              h->c, vp, d_arrows);
+                                              h->nbr, h->c, vp, d_arrows);
       break;
     case OS_STORAGE_F16:
       k_render_arrows<__half><<<g, b, 0, st>>>((const __half*)h->u, (const __half*)h->v,
-                                               h->flags, h->c, vp, d_arrows);
+                                               h->flags, h->nbr, h->c, vp, d_arrows);
       break;
     case OS_STORAGE_BF16:
       k_render_arrows<__nv_bfloat16><<<g, b, 0, st>>>(
-          (const __nv_bfloat16*)h->u, (const __nv_bfloat16*)h->v, h->flags, h->c, vp, d_arrows);
+          (const __nv_bfloat16*)h->u, (const __nv_bfloat16*)h->v, h->flags, h->nbr, h->c, vp, d_arrows);
       break;
     default:
       return set_err(OS_ERR_UNSUPPORTED, "visuals need FP32, FP16 or BF16 storage");
@@ -1197,16 +1203,16 @@ int os_render_traces(os_handle* h, const os_visual_config* v, float dt, int32_t*
   switch (h->storage) {
     case OS_STORAGE_F32:
       k_render_traces<float><<<g, b, 0, st>>>((const float*)h->u, (const float*)h->v, h->flags,
-                                              h->c, vp, dt, d_x, d_y);
+                                              h->nbr, h->c, vp, dt, d_x, d_y);
       break;
     case OS_STORAGE_F16:
       k_render_traces<__half><<<g, b, 0, st>>>((const __half*)h->u, (const __half*)h->v,
-                                               h->flags, h->c, vp, dt, d_x, d_y);
+                                               h->flags, h->nbr, h->c, vp, dt, d_x, d_y);
       break;
     case OS_STORAGE_BF16:
       k_render_traces<__nv_bfloat16><<<g, b, 0, st>>>((const __nv_bfloat16*)h->u,
-                                                      (const __nv_bfloat16*)h->v, h->flags, h->c,
-                                                      vp, dt, d_x, d_y);
+                                                      (const __nv_bfloat16*)h->v, h->flags, h->nbr,
+                                                      h->c, vp, dt, d_x, d_y);
       break;
     default:
       return set_err(OS_ERR_UNSUPPORTED, "visuals need FP32, FP16 or BF16 storage");

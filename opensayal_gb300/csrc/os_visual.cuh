@@ -137,8 +137,8 @@ struct VisualParams {
 // buffer (before it, for the rows); here the entry index itself is bounded.
 template <class S>
 __global__ void k_render_arrows(const S* __restrict__ u, const S* __restrict__ v,
-                                const uint8_t* __restrict__ fl, Consts c, VisualParams vp,
-                                os_arrow* __restrict__ arrows) {
+                                const uint8_t* __restrict__ fl, const uint16_t* __restrict__ nb,
+                                Consts c, VisualParams vp, os_arrow* __restrict__ arrows) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   int j = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= vp.arrows_w || j >= vp.arrows_h) return;
@@ -150,8 +150,8 @@ __global__ void k_render_arrows(const S* __restrict__ u, const S* __restrict__ v
   const float x = centre(0.0f, i, vp.cell_px);
   const float y = centre(0.0f, c.H - j - 1, vp.cell_px);
   const float sy = c.H * vp.cell_px - y;
-  const float vel_x = sample_u<S, float>(c, fl, u, x, sy);
-  const float vel_y = sample_v<S, float>(c, fl, v, x, sy);
+  const float vel_x = sample_u<S, float>(c, nb, u, x, sy);
+  const float vel_y = sample_v<S, float>(c, nb, v, x, sy);
   const float angle = atan2f(vel_y, vel_x);
   float length = sqrtf(vel_x * vel_x + vel_y * vel_y);
   os_arrow a;
@@ -187,8 +187,9 @@ __global__ void k_render_arrows(const S* __restrict__ u, const S* __restrict__ v
 // arrows' is (the reference bounds only the cell).
 template <class S>
 __global__ void k_render_traces(const S* __restrict__ u, const S* __restrict__ v,
-                                const uint8_t* __restrict__ fl, Consts c, VisualParams vp,
-                                float d_t, int* __restrict__ xs, int* __restrict__ ys) {
+                                const uint8_t* __restrict__ fl, const uint16_t* __restrict__ nb,
+                                Consts c, VisualParams vp, float d_t, int* __restrict__ xs,
+                                int* __restrict__ ys) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   int j = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= vp.traces_w || j >= vp.traces_h) return;
@@ -206,8 +207,8 @@ __global__ void k_render_traces(const S* __restrict__ u, const S* __restrict__ v
   xs[base] = static_cast<int>(roundf(px));
   ys[base] = c.H - 1 - static_cast<int>(roundf(py));
   for (int k = 1; k < vp.trace_length; k++) {
-    const float vx = sample_u<S, float>(c, fl, u, px, py);
-    const float vy = sample_v<S, float>(c, fl, v, px, py);
+    const float vx = sample_u<S, float>(c, nb, u, px, py);
+    const float vy = sample_v<S, float>(c, nb, v, px, py);
     px = px + vx * d_t;
     py = py + vy * d_t;
     xs[base + k] = static_cast<int>(roundf(px));
