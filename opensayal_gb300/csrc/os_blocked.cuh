@@ -767,6 +767,24 @@ __device__ __forceinline__ void diff_stage_in(float* A, float* B, int tx, int ty
   }
 }
 
+// One column's run of Jacobi updates, rows e0, e0 + rs, ... (n of them), from
+// A into B. The buffers never overlap, so the loads of later rows may be
+// issued ahead of earlier rows' stores.
+__device__ __forceinline__ void diff_column(const float* __restrict__ A, float* __restrict__ B,
+                                            int e0, int rs, int n, float a, float den) {
+  float down = A[e0 - rs];
+  float centre = A[e0];
+  int e = e0;
+#pragma unroll 4
+  for (int t = 0; t < n; t++, e += rs) {
+    const float up = A[e + rs];
+    // src/fluid.cu:178-182: neighbours (i-1, j), (i+1, j), (i, j-1), (i, j+1)
+    B[e] = fma_rn(a, A[e - 1] + A[e + 1] + down + up, centre) / den;
+    down = centre;
+    centre = up;
+  }
+}
+
 // `sweeps` Jacobi sweeps on the staged region, A -> B -> A ...; on return A
 // holds the result (the pointers are swapped as the sweeps go). Ends with a
 // barrier. With FLIP the region's rows are stored top row first (the order
@@ -792,6 +810,7 @@ __device__ __forceinline__ void diff_sweeps(float*& A, float*& B, int tx, int ty
   const int r0 = y_lo + (threadIdx.x / kRegionW) * chunk;
   const int r1 = min(y_hi + 1, r0 + chunk);
   const bool column = x > 0 && x < kRegionW - 1 && i > 0 && i < W - 1 && r0 < r1;
+  const float den = fma_rn(4.0f, a, 1.0f);
   for (int t = 0; t < sweeps; t++) {
     // Only cells within `reach` (sweeps still to come) of the owned tile can
     // still influence it.
@@ -800,16 +819,7 @@ __device__ __forceinline__ void diff_sweeps(float*& A, float*& B, int tx, int ty
     if (column && x >= halo - reach && x < kRegionW - halo + reach && ya < yb) {
       const int rs = FLIP ? -kRegionW : kRegionW;     // step to the next region row
       const int base = FLIP ? (RH - 1) * kRegionW : 0;
-      float down = A[base + (ya - 1) * rs + x];
-      float centre = A[base + ya * rs + x];
-      for (int y = ya; y < yb; y++) {
-        const int e = base + y * rs + x;
-        const float up = A[e + rs];
-        // src/fluid.cu:178-182: neighbours (i-1, j), (i+1, j), (i, j-1), (i, j+1)
-        B[e] = fma_rn(a, A[e - 1] + A[e + 1] + down + up, centre) / fma_rn(4.0f, a, 1.0f);
-        down = centre;
-        centre = up;
-      }
+      diff_column(A, B, base + ya * rs + x, rs, yb - ya, a, den);
     }
     __syncthreads();
     float* T = A;
