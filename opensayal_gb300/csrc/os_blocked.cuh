@@ -490,11 +490,13 @@ __device__ __forceinline__ void vreg_half_sweep(const ProjPlanes& P, float (&v)[
   const uint32_t rows = ((1u << rhi) - 1u) & ~((1u << rlo) - 1u);
   const bool col_ok[2] = {2 * p >= lo && 2 * p < x_end, 2 * p + 1 >= lo && 2 * p + 1 < x_end};
   constexpr int ca = COLOUR & 1, cb = ca ^ 1;   // active columns of even and odd rows
+  // Rows whose active cell of this thread's pair is in the cone.
+  const uint32_t live = rows & ((col_ok[ca] ? 0x55555555u : 0u) | (col_ok[cb] ? 0xaaaaaaaau : 0u));
 #pragma unroll
   for (int r = 0; r < R; r += 2) {
     if (((rows >> r) & 3u) == 0u) continue;  // both rows off the cone: the same for the warp
-    const bool ia = ((rows >> r) & 1u) && col_ok[ca];
-    const bool ib = ((rows >> (r + 1)) & 1u) && col_ok[cb];
+    const bool ia = (live >> r) & 1u;
+    const bool ib = (live >> (r + 1)) & 1u;
     if constexpr (PRESSURE) {
       vreg_row<ca, PRESSURE, R>(P, v, vt, p, y0, r, ia, c, d_t);
       vreg_row<cb, PRESSURE, R>(P, v, vt, p, y0, r + 1, ib, c, d_t);
@@ -505,15 +507,14 @@ __device__ __forceinline__ void vreg_half_sweep(const ProjPlanes& P, float (&v)[
     float* uRa = ca ? P.ue + ea + 1 : P.uo + ea;
     float* uLb = (cb ? P.uo : P.ue) + eb;
     float* uRb = cb ? P.ue + eb + 1 : P.uo + eb;
-    const uint32_t fa = ia ? (ca ? P.fo : P.fe)[ea] : 0u;
-    const uint32_t fb = ib ? (cb ? P.fo : P.fe)[eb] : 0u;
-    float a0 = ia ? *uLa : 0.0f, a1 = ia ? *uRa : 0.0f;
-    float b0 = ib ? *uLb : 0.0f, b1 = ib ? *uRb : 0.0f;
+    // Both rows of a pair that is not skipped lie inside the region (RH and the
+    // strips' first rows are even, and the cone ends below row RH - 1), so the
+    // loads need no predicate; only the updates and the stores do.
+    const uint32_t fa = ia ? (uint32_t)(ca ? P.fo : P.fe)[ea] : 0u;
+    const uint32_t fb = ib ? (uint32_t)(cb ? P.fo : P.fe)[eb] : 0u;
+    float a0 = *uLa, a1 = *uRa;
+    float b0 = *uLb, b1 = *uRb;
     float pa = 0.0f, pb = 0.0f;
-    if (PRESSURE) {
-      pa = ia ? (ca ? P.po : P.pe)[ea] : 0.0f;
-      pb = ib ? (cb ? P.po : P.pe)[eb] : 0.0f;
-    }
     float& top_b = (r + 2 < R) ? v[cb][r + 2] : vt[cb];
     project_faces_sel<PRESSURE>(fa, c, d_t, a0, a1, v[ca][r], v[ca][r + 1], pa);
     project_faces_sel<PRESSURE>(fb, c, d_t, b0, b1, v[cb][r + 1], top_b, pb);
