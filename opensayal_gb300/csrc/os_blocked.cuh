@@ -443,10 +443,10 @@ __device__ __forceinline__ void project_faces_sel(uint32_t f, const Consts& c, f
     const float np = pc + velocity_diff * c.density * (float)c.h / d_t;
     pc = f ? np : pc;
   }
-  uc = (f & F_LEFT) ? uc + velocity_diff : uc;
-  right_u = (f & F_RIGHT) ? right_u - velocity_diff : right_u;
-  vc = (f & F_BOTTOM) ? vc + velocity_diff : vc;
-  top_v = (f & F_TOP) ? top_v - velocity_diff : top_v;
+  if (f & F_LEFT) uc = uc + velocity_diff;
+  if (f & F_RIGHT) right_u = right_u - velocity_diff;
+  if (f & F_BOTTOM) vc = vc + velocity_diff;
+  if (f & F_TOP) top_v = top_v - velocity_diff;
 }
 
 // One row of a half-sweep, with branches (the accumulated pressure needs the
