@@ -141,9 +141,12 @@ __global__ void k_batch_forces(const PlanHeader* __restrict__ P, const int* __re
   for_cells(P, remaining, [&](const ScenarioDesc& d, int j, int i0, int i1) {
     with_storage(d.storage, [&](auto tag) {
       using S = std::remove_pointer_t<decltype(tag)>;
-      for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x)
-        forces_cell<S, float>(static_cast<S*>(d.u), static_cast<S*>(d.v), static_cast<S*>(d.s),
-                              d.c, d.smoke_period, d.prm, i, j);
+      S* v = static_cast<S*>(d.v);
+      for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+        const int64_t k = cell_index(d.c.W, d.c.H, i, j);
+        st(v + k, forces_cell<S, float>(static_cast<S*>(d.u), static_cast<S*>(d.s),
+                                        ld<float>(v + k), d.c, d.smoke_period, d.prm, i, j));
+      }
     });
   });
 }
