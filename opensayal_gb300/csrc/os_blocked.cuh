@@ -201,12 +201,10 @@ __device__ __forceinline__ ProjPlanes proj_planes(float* smem, int RH) {
   return P;
 }
 
-// One colour half-sweep over the region. Active cells of row y sit at
-// x = 2k + par with par = (y + COLOUR) & 1 (region origin has even global
-// coordinates, so local parity is global parity). A thread keeps one k and
-// steps through rows 2*(blockDim/128) apart, so its parity, and with it every
-// plane offset, is fixed for the whole loop. Planes are addressed as word
-// offsets from the __shared__ base: ue 0, uo 1, ve 2, vo 3, pe 4, po 5 (x plane).
+// Colours: the active cells of region row y in half-sweep COLOUR sit at
+// x = 2k + ((y + COLOUR) & 1) (the region origin has even global coordinates,
+// so local parity is global parity).
+//
 // A cell's flag byte as the blocked sweeps keep it in shared memory: 0 for a
 // cell the projection does not update (not F_ACTIVE); otherwise bit 0 set, the
 // neighbour bits F_LEFT .. F_TOP in place, and in bits 5-7 the number of
@@ -428,21 +426,15 @@ __device__ __forceinline__ void proj_sweeps(float* smem, const Consts& c,
 // after the barrier the other side reads it. The word is next written by the
 // side that just read it, so one barrier per half-sweep suffices.
 // ---------------------------------------------------------------------------
-// project_faces without branches, for cells taken two rows at a time: `f` is
-// the sweep flag byte, 0 for any cell not updated (inactive, off the cone or
-// off the region), whose faces then keep their values. The expressions are
-// project_faces' own.
-template <bool PRESSURE>
-__device__ __forceinline__ void project_faces_sel(uint32_t f, const Consts& c, float d_t,
-                                                  float& uc, float& right_u, float& vc,
-                                                  float& top_v, float& pc) {
+// project_faces without branches and without the pressure, for cells taken
+// two rows at a time: `f` is the sweep flag byte, 0 for any cell not updated
+// (inactive, off the cone or off the region), whose faces then keep their
+// values. The expressions are project_faces' own.
+__device__ __forceinline__ void project_faces_sel(uint32_t f, const Consts& c, float& uc,
+                                                  float& right_u, float& vc, float& top_v) {
   const float divergence = right_u - uc + top_v - vc;
   const int sn = (int)(f >> kSweepCountShift);
   const float velocity_diff = mul_rn(c.o, divergence / (float)sn);
-  if (PRESSURE) {
-    const float np = pc + velocity_diff * c.density * (float)c.h / d_t;
-    pc = f ? np : pc;
-  }
   if (f & F_LEFT) uc = uc + velocity_diff;
   if (f & F_RIGHT) right_u = right_u - velocity_diff;
   if (f & F_BOTTOM) vc = vc + velocity_diff;
@@ -474,7 +466,8 @@ __device__ __forceinline__ void vreg_row(const ProjPlanes& P, float (&v)[2][R], 
 // One colour half-sweep over the thread's strip. Rows go two at a time (the
 // two active cells sit in different columns and share no face): both rows'
 // loads first, then both updates, then both stores, with no branches, so the
-// two dependency chains overlap. A pair of rows wholly outside the cone or
+// two dependency chains overlap (with the pressure on, each row on its own,
+// vreg_row). A pair of rows wholly outside the cone or
 // the region is skipped (a branch that is the same for the whole warp); a
 // single such row, or a column off the cone, is predicated off. An inactive
 // cell in the cone stores its faces unchanged (no other cell of the colour
@@ -507,26 +500,23 @@ __device__ __forceinline__ void vreg_half_sweep(const ProjPlanes& P, float (&v)[
     float* uRa = ca ? P.ue + ea + 1 : P.uo + ea;
     float* uLb = (cb ? P.uo : P.ue) + eb;
     float* uRb = cb ? P.ue + eb + 1 : P.uo + eb;
-    // Both rows of a pair that is not skipped lie inside the region (RH and the
-    // strips' first rows are even, and the cone ends below row RH - 1), so the
-    // loads need no predicate; only the updates and the stores do.
+    // Both rows of a pair that is not skipped lie inside the region (the cone
+    // ends below row RH - 1), so the loads need no predicate; only the updates
+    // and the stores do.
     const uint32_t fa = ia ? (uint32_t)(ca ? P.fo : P.fe)[ea] : 0u;
     const uint32_t fb = ib ? (uint32_t)(cb ? P.fo : P.fe)[eb] : 0u;
     float a0 = *uLa, a1 = *uRa;
     float b0 = *uLb, b1 = *uRb;
-    float pa = 0.0f, pb = 0.0f;
     float& top_b = (r + 2 < R) ? v[cb][r + 2] : vt[cb];
-    project_faces_sel<PRESSURE>(fa, c, d_t, a0, a1, v[ca][r], v[ca][r + 1], pa);
-    project_faces_sel<PRESSURE>(fb, c, d_t, b0, b1, v[cb][r + 1], top_b, pb);
+    project_faces_sel(fa, c, a0, a1, v[ca][r], v[ca][r + 1]);
+    project_faces_sel(fb, c, b0, b1, v[cb][r + 1], top_b);
     if (ia) {
       *uLa = a0;
       *uRa = a1;
-      if (PRESSURE) (ca ? P.po : P.pe)[ea] = pa;
     }
     if (ib) {
       *uLb = b0;
       *uRb = b1;
-      if (PRESSURE) (cb ? P.po : P.pe)[eb] = pb;
     }
   }
   // Boundary faces this half-sweep may have changed, for the neighbouring strip.
