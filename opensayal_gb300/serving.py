@@ -84,11 +84,14 @@ class Server:
 
     max_members bounds the requests on the GPU at once (the batch's step time
     grows with their cells); chunk is the number of steps enqueued per loop
-    turn and depth the chunks allowed in flight before the loop waits."""
+    turn and depth the chunks allowed in flight before the loop waits. `batch`
+    replaces the dynamic Batch the server would create (any object with its
+    add/remove/step/wait/poll/status/memory/scenario/stats/synchronize)."""
 
     def __init__(self, budget_bytes: int, block_k: int = 8, max_members: int = 64,
-                 chunk: int = 2, depth: int = 2, device: int = 0):
-        self.batch = Batch.dynamic(block_k=block_k, device=device, budget_bytes=budget_bytes)
+                 chunk: int = 2, depth: int = 2, device: int = 0, batch=None):
+        self.batch = batch if batch is not None else Batch.dynamic(
+            block_k=block_k, device=device, budget_bytes=budget_bytes)
         self.max_members = max_members
         self.chunk = chunk
         self.depth = depth
@@ -103,7 +106,7 @@ class Server:
         self.close()
 
     def run(self, requests: list[Request], horizon_s: float, results: dict | None = None,
-            clock=time.perf_counter) -> ServeReport:
+            clock=time.perf_counter, sleep=time.sleep) -> ServeReport:
         b = self.batch
         rep = ServeReport()
         pending = deque(sorted(requests, key=lambda r: r.arrival))
@@ -146,7 +149,7 @@ class Server:
             if now >= horizon_s or (not pending and not queue and not active):
                 break
             if not active and not queue and pending:
-                time.sleep(max(0.0, min(pending[0].arrival - now, horizon_s - now)))
+                sleep(max(0.0, min(pending[0].arrival - now, horizon_s - now)))
         # Progress of the unfinished members counts toward the served work.
         b.synchronize()
         for mid, (req, _) in active.items():
