@@ -11,7 +11,7 @@ Bars (relative L2 unless stated):
   racing threads, the library runs Jacobi; they differ by <= 64 a^2 per sweep
   (a = viscosity*dt/h^2);
 * 100 full FP32 steps of the 256x128 case against the reference kernels:
-  1e-5 (the spec bar). With the drain open the reference races on
+  1e-5 (the bar this path is held to). With the drain open the reference races on
   v(W-1, 1) (src/fluid.cu:720-733) and two runs of the reference itself
   differ by up to ~3e-5, so that variant is held to 1e-4;
 * against the CPU oracle: 1e-5 per phase and for inviscid runs; viscous runs
