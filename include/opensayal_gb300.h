@@ -133,7 +133,9 @@ typedef struct os_config {
                                0 = projection_block's depth, or with
                                projection_block 0 the autotuner's choice
                                (its halo is K cells against the projection's
-                               2K, so deeper passes can pay) */
+                               2K, so deeper passes can pay). Single handles
+                               only: a batch runs its own depth for every
+                               member */
   int32_t reserved[2];
 } os_config;
 
