@@ -117,3 +117,24 @@ def test_batched_scenarios_distribution(lib_built):
         assert c.width // 4 <= c.obstacle_center_x <= 3 * c.width // 4
         assert 4.0 <= c.obstacle_radius <= 0.1 * c.height
         assert -10.0 <= c.g <= 0.0 and c.projection_n in (50, 100, 200)
+
+
+def test_serving_requests_distribution(lib_built):
+    """Poisson arrivals at 200/s for 60 s: about 12,000 requests in order, the
+    batched scenario mix, steps in [100, 5000], half in BF16 storage."""
+    reqs = scenarios.serving_requests(200.0, 60.0, seed=5)
+    n = len(reqs)
+    assert abs(n - 12000) < 5 * np.sqrt(12000)
+    t = np.array([r.arrival for r in reqs])
+    assert (np.diff(t) > 0).all() and t[0] > 0 and t[-1] < 60.0
+    gaps = np.diff(t)
+    assert abs(gaps.mean() - 1 / 200.0) < 0.1 / 200.0  # exponential gaps, mean 1/rate
+    steps = np.array([r.steps for r in reqs])
+    assert steps.min() >= 100 and steps.max() <= 5000
+    assert abs(steps.mean() - 2550) < 100
+    bf16 = np.mean([r.config.storage == 2 for r in reqs])
+    assert 0.45 < bf16 < 0.55
+    assert all(r.index == k for k, r in enumerate(reqs))
+    assert len({r.seed for r in reqs}) == n  # one perturbation seed per request
+    again = scenarios.serving_requests(200.0, 60.0, seed=5)
+    assert [(r.arrival, r.steps) for r in again] == [(r.arrival, r.steps) for r in reqs]
