@@ -174,15 +174,15 @@ def workload_config(name: str):
             "large": scenarios.large_config}[name]()
 
 
-def config_record(cfg, name: str, extra: dict) -> dict:
-    rec = {"workload": f"{name}: {cfg.width}x{cfg.height} tunnel, n={cfg.projection_n}, "
-                       f"o={cfg.projection_o:g}, viscosity={cfg.viscosity:g}, g={cfg.g:g}, "
-                       f"dt={cfg.d_t:g}, drain={cfg.enable_drain}, smoke={cfg.enable_smoke}",
-           "width": cfg.width, "height": cfg.height, "projection_n": cfg.projection_n,
-           "storage": ["f32", "f16", "bf16", "f64"][cfg.storage],
-           "l2": "flushed between steps (256 MiB write outside the timed events)"}
-    rec.update(extra)
-    return rec
+def config_record(cfg, name: str, world: int) -> dict:
+    """The workload, and only the workload: both arms print the same record."""
+    return {"workload": f"{name}: {cfg.width}x{cfg.height} tunnel, n={cfg.projection_n}, "
+                        f"o={cfg.projection_o:g}, viscosity={cfg.viscosity:g}, g={cfg.g:g}, "
+                        f"dt={cfg.d_t:g}, drain={cfg.enable_drain}, smoke={cfg.enable_smoke}",
+            "width": cfg.width, "height": cfg.height, "projection_n": cfg.projection_n,
+            "storage": ["f32", "f16", "bf16", "f64"][cfg.storage],
+            "l2": "GPU steps: flushed between timed steps (256 MiB write outside the events)",
+            "parallelism": "replicas" if world > 1 else "single", "global_batch": world}
 
 
 def time_visuals(f, cfg, sptr, stream, pk) -> dict:
@@ -306,12 +306,11 @@ def run_gb300(args, world, rank, local) -> dict | None:
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": ["f32", "f16", "bf16", "f64"][cfg.storage], "data": "synthetic",
-        "config": config_record(cfg, args.workload, {
-            "parallelism": "replicas" if world > 1 else "single", "global_batch": world,
-            "kernels_per_step": launches // max(1, args.steps),
-            "projection_block": f.fields().projection_block,
-            "projection_resident": f.fields().projection_resident,
-            "projection_block_source": "autotuned" if cfg.projection_block == 0 else "fixed"}),
+        "config": config_record(cfg, args.workload, world),
+        "tuning": {"kernels_per_step": launches // max(1, args.steps),
+                   "projection_block": f.fields().projection_block,
+                   "projection_resident": f.fields().projection_resident,
+                   "projection_block_source": "autotuned" if cfg.projection_block == 0 else "fixed"},
         "e2e": e2e,
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"],
@@ -327,31 +326,49 @@ def run_gb300(args, world, rank, local) -> dict | None:
         "clocks": clk.summary(),
     }
     result["visual"] = time_visuals(f, cfg, sptr, stream, pk)
+    f.close()
+    del flush
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline(cfg)
-    f.close()
+    if args.workload == "default" and not args.no_legs:
+        # The other two legs of the metric: batched uneven tunnels and served
+        # Poisson arrivals, each against one-at-a-time solves on the same GPU.
+        result["batched"] = batched_measure(world, rank, local, args.scenarios, args.steps,
+                                            args.warmup, baselines=not args.no_cpu_baseline)
+        result["serving"] = serving_measure(world, rank, local, args.leg_serve_rate,
+                                            args.leg_serve_seconds, args.leg_serve_drain,
+                                            args.serve_budget_gb, args.serve_slots,
+                                            args.serve_chunk, serial=not args.no_serial)
     return result if rank == 0 else None
 
 
-def run_batched(args, world, rank, local) -> dict | None:
-    """512 uneven tunnels (seed 4): W, H in {128..1024}, n in {50, 100, 200},
-    advanced together by one graph per step, against the same scenarios run
-    one at a time (the plain per-sweep launch sequence the reference uses, and
-    this library's blocked engine)."""
+BATCHED_WORKLOAD = ("batched: {count} uneven tunnels (seed 4), W,H in 128..1024 step 32, "
+                    "n in {{50,100,200}}, pipe H/4, inflow U[0.5,3], dt 0.05")
+
+
+def batched_measure(world, rank, local, count: int, steps: int, warmup: int, *,
+                    mixed: bool = False, block: int = 0, sample_every: int = 8,
+                    baselines: bool = True) -> dict:
+    """The batched scenarios (seed 4): `count` uneven tunnels advanced together
+    by one graph per step, timed over `steps` steps with CUDA events; then,
+    every step, the batch step plus every scenario's smoke read back (e2e);
+    then, on every `sample_every`-th scenario, the same scenarios one at a time
+    (this library's plain per-sweep launch sequence, which is the reference's
+    launch pattern and synchronises every step, and its blocked handles)."""
     import torch
     from opensayal_gb300 import Fluid, scenarios
     from opensayal_gb300.batch import Batch
     from opensayal_gb300.build import build_library
     build_library()
     torch.cuda.set_device(local)
-    count = args.scenarios
     cfgs = scenarios.batched_scenarios(count, seed=4 + 1000 * rank)
     for i, c in enumerate(cfgs):
         c.device = local
-        if args.mixed and i % 2:
+        if mixed and i % 2:
             c.storage = 2  # OS_STORAGE_BF16
     cells = sum(c.width * c.height for c in cfgs)
-    b = Batch(cfgs, block_k=args.block if args.block and args.block > 0 else 0)
+    t_setup = time.perf_counter()
+    b = Batch(cfgs, block_k=block if block and block > 0 else 0)
     for i, c in enumerate(cfgs):
         view = b.scenario(i)
         u, v = scenarios.perturbation(4000 + i, view.download("is_solid"))
@@ -359,26 +376,28 @@ def run_batched(args, world, rank, local) -> dict | None:
         view.upload("vel_y", v)
     stream = torch.cuda.Stream()
     sptr = stream.cuda_stream
-    b.step(args.warmup, sptr)
+    b.step(warmup, sptr)
     stream.synchronize()
+    setup_s = time.perf_counter() - t_setup
     launches0 = b.stats().launches
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     dist_barrier(world)
     torch.cuda.synchronize()
     with Clocks(local) as clk:
         start.record(stream)
-        b.step(args.steps, sptr)
+        b.step(steps, sptr)
         end.record(stream)
         torch.cuda.synchronize()
     dist_barrier(world)
     total_s = dist_max(world, start.elapsed_time(end) / 1e3)
-    value = world * cells * args.steps / total_s
+    value = world * cells * steps / total_s
     st = b.stats()
+    launches = int(st.launches - launches0)
 
     # e2e: every step, the batch step plus every scenario's smoke read back
     pinned = torch.empty(max(c.width * c.height for c in cfgs), dtype=torch.float32,
                          pin_memory=True).numpy()
-    e2e_steps = min(args.steps, 5)
+    e2e_steps = min(steps, 5)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         b.step(1)
@@ -386,64 +405,88 @@ def run_batched(args, world, rank, local) -> dict | None:
         for i, c in enumerate(cfgs):
             b.scenario(i).download("smoke", out=pinned[: c.width * c.height])
     e2e_s = dist_max(world, time.perf_counter() - t0)
+    b.close()
 
-    # the same scenarios one at a time: plain per-sweep kernels (the
-    # reference's launch pattern, synchronising per step) and blocked handles
-    def one_at_a_time(block: int, steps: int) -> float:
+    def one_at_a_time(block_k: int, sample: list, per: int) -> float:
         t = 0.0
         done = 0
-        for c in cfgs:
+        for c in sample:
             cc = c.copy()
-            cc.projection_block = block
+            cc.projection_block = block_k
             with Fluid(cc) as f:
                 f.update(None, cc.d_t)
                 t1 = time.perf_counter()
-                for _ in range(steps):
+                for _ in range(per):
                     f.update(None, cc.d_t)
                 t += time.perf_counter() - t1
-                done += cc.width * cc.height * steps
+                done += cc.width * cc.height * per
         return done / t
 
-    plain = one_at_a_time(-1, 2) if not args.no_cpu_baseline else None
-    alone = one_at_a_time(8, 2) if not args.no_cpu_baseline else None
-    b.close()
+    alone = None
+    if baselines:
+        sample = cfgs[::sample_every]
+        alone = {"plain_per_sweep_sync": one_at_a_time(-1, sample, 2),
+                 "blocked_graph_sync": one_at_a_time(8, sample, 2), "unit": UNIT,
+                 "steps_per_scenario": 2,
+                 "sample": f"every {sample_every}th scenario ({len(sample)} of {count}), "
+                           "host wall clock around synchronous updates"}
+    return {
+        "value": value, "unit": UNIT, "steps": steps, "warmup": warmup,
+        "ms_per_step": total_s * 1e3 / steps,
+        "workload": BATCHED_WORKLOAD.format(count=count) + (" (BF16 for half)" if mixed else ""),
+        "scenarios": count, "cells": cells, "setup_s": setup_s,
+        "tuning": {"block_k": st.block_k, "kernels_per_step": st.kernels_per_step,
+                   "tile_items_per_step": st.tile_items_per_step},
+        "l2": f"inputs larger than L2 ({cells * 37 / 1e9:.1f} GB of fields)",
+        "e2e": {"value": world * cells * e2e_steps / e2e_s, "unit": UNIT,
+                "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 4 * cells,
+                "steps": e2e_steps},
+        "gpu_launches": launches,
+        "one_at_a_time": alone,
+        "clocks": clk.summary(),
+    }
+
+
+def run_batched(args, world, rank, local) -> dict | None:
+    """The batched scenarios as the line's own workload (--workload batched)."""
+    m = batched_measure(world, rank, local, args.scenarios, args.steps, args.warmup,
+                        mixed=args.mixed, block=args.block or 0,
+                        baselines=not args.no_cpu_baseline)
     res = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": total_s * 1e3 / args.steps,
+        "metric": METRIC, "value": m["value"], "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": m["ms_per_step"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32/bf16" if args.mixed else "f32", "data": "synthetic",
-        "config": {"workload": f"batched{' mixed BF16/FP32' if args.mixed else ''}: {count} uneven tunnels (seed 4), W,H in 128..1024 step "
-                               f"32, n in {{50,100,200}}, dt 0.05", "scenarios": count,
-                   "cells": cells, "block_k": st.block_k, "kernels_per_step": st.kernels_per_step,
-                   "tile_items_per_step": st.tile_items_per_step,
-                   "l2": f"inputs larger than L2 ({cells * 37 / 1e9:.1f} GB of fields)",
-                   "parallelism": "replicas" if world > 1 else "single"},
-        "e2e": {"value": world * cells * e2e_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 0,
-                "d2h_bytes_per_step": 4 * cells},
-        "gpu_launches": int(st.launches - launches0),
-        "one_at_a_time": {"plain_per_sweep_sync": plain, "blocked_graph_sync": alone,
-                          "unit": UNIT, "steps_per_scenario": 2},
-        "clocks": clk.summary(),
+        "config": {"workload": m["workload"], "scenarios": m["scenarios"], "cells": m["cells"],
+                   "l2": m["l2"], "parallelism": "replicas" if world > 1 else "single"},
+        "tuning": m["tuning"], "e2e": m["e2e"], "gpu_launches": m["gpu_launches"],
+        "one_at_a_time": m["one_at_a_time"], "clocks": m["clocks"],
     }
     return res if rank == 0 else None
 
 
-def run_serving(args, world, rank, local) -> dict | None:
+SERVING_WORKLOAD = ("serving: Poisson {rate:g}/s for {seconds:g} s (seed 5), tunnels as batched, "
+                    "steps U[100,5000], BF16 storage p=0.5")
+
+
+def serving_measure(world, rank, local, rate: float, seconds: float, drain: float,
+                    budget_gb: float, slots: int, chunk: int, serial: bool = True) -> dict:
     """Poisson arrivals (seed 5) of tunnels drawn as in the batched workload,
     steps U[100, 5000], BF16 or FP32 storage (p = 0.5), served by continuous
     batching within a device-memory budget; the same arrival trace served one
-    request at a time by single handles is the baseline. Both run to the same
-    horizon (arrival window plus a drain allowance)."""
+    request at a time by single handles is the baseline. Both stop at the
+    horizon (arrival window plus a drain allowance) or when every request is
+    done."""
     import torch
     from opensayal_gb300 import scenarios
     from opensayal_gb300.build import build_library
     from opensayal_gb300.serving import Server, serve_serial
     build_library()
     torch.cuda.set_device(local)
-    reqs = scenarios.serving_requests(args.serve_rate, args.serve_seconds, seed=5 + 1000 * rank)
+    reqs = scenarios.serving_requests(rate, seconds, seed=5 + 1000 * rank)
     for r in reqs:
         r.config.device = local
-    horizon = args.serve_seconds + args.serve_drain
+    horizon = seconds + drain
     # Warm the library and the graph path on two small requests first.
     warm = scenarios.serving_requests(1000.0, 0.002, seed=99)[:2]
     for r in warm:
@@ -451,37 +494,48 @@ def run_serving(args, world, rank, local) -> dict | None:
         r.steps = 3
     with Server(budget_bytes=1 << 30, block_k=8, max_members=2) as w:
         w.run(warm, 60.0)
-    budget = int(args.serve_budget_gb * 1e9)
+    budget = int(budget_gb * 1e9)
     dist_barrier(world)
     with Clocks(local) as clk:
-        with Server(budget_bytes=budget, block_k=8, max_members=args.serve_slots,
-                    chunk=args.serve_chunk) as srv:
+        with Server(budget_bytes=budget, block_k=8, max_members=slots, chunk=chunk) as srv:
             rep = srv.run(reqs, horizon)
             st = srv.batch.stats()
     served = rep.summary()
-    serial = None
-    if not args.no_serial:
-        serial = serve_serial(reqs, horizon, block_k=8).summary()
+    serial_rep = serve_serial(reqs, horizon, block_k=8).summary() if serial else None
     value = dist_sum(world, float(rep.cell_steps)) / dist_max(world, rep.wall_s)
-    res = {
-        "metric": "served cell-steps/s (continuous batching, Poisson arrivals)",
-        "value": value, "unit": UNIT, "n_gpus": world, "steps": int(st.steps_enqueued),
-        "warmup": 1, "ms_per_step": rep.wall_s * 1e3 / max(1, st.steps_enqueued),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32/bf16",
-        "data": "synthetic",
-        "config": {"workload": f"serving: Poisson {args.serve_rate}/s for {args.serve_seconds} s "
-                               f"(seed 5), tunnels as batched, steps U[100,5000], BF16 p=0.5",
-                   "budget_gb": args.serve_budget_gb, "max_members": args.serve_slots,
-                   "chunk": args.serve_chunk, "horizon_s": horizon, "block_k": st.block_k,
-                   "l2": "inputs larger than L2 (tens of members, ~12 MB each)",
-                   "parallelism": "replicas" if world > 1 else "single"},
-        "serving": served,
-        "serial_plain": serial,
+    return {
+        "value": value, "unit": UNIT,
+        "workload": SERVING_WORKLOAD.format(rate=rate, seconds=seconds),
+        "budget_gb": budget_gb, "max_members": slots, "chunk": chunk, "horizon_s": horizon,
+        "block_k": st.block_k, "requests": len(reqs),
+        "serving": served, "serial_single_handles": serial_rep,
         "e2e": {"value": value, "unit": UNIT,
                 "h2d_bytes_per_step": rep.h2d_bytes // max(1, st.steps_enqueued),
                 "d2h_bytes_per_step": rep.d2h_bytes // max(1, st.steps_enqueued)},
-        "gpu_launches": int(st.launches),
-        "clocks": clk.summary(),
+        "gpu_launches": int(st.launches), "steps_enqueued": int(st.steps_enqueued),
+        "wall_s": rep.wall_s, "clocks": clk.summary(),
+    }
+
+
+def run_serving(args, world, rank, local) -> dict | None:
+    """The served scenarios as the line's own workload (--workload serving)."""
+    m = serving_measure(world, rank, local, args.serve_rate, args.serve_seconds,
+                        args.serve_drain, args.serve_budget_gb, args.serve_slots,
+                        args.serve_chunk, serial=not args.no_serial)
+    steps = max(1, m["steps_enqueued"])
+    res = {
+        "metric": "served cell-steps/s (continuous batching, Poisson arrivals)",
+        "value": m["value"], "unit": UNIT, "n_gpus": world, "steps": steps,
+        "warmup": 1, "ms_per_step": m["wall_s"] * 1e3 / steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32/bf16",
+        "data": "synthetic",
+        "config": {"workload": m["workload"], "budget_gb": m["budget_gb"],
+                   "max_members": m["max_members"], "chunk": m["chunk"],
+                   "horizon_s": m["horizon_s"],
+                   "l2": "inputs larger than L2 (tens of members, ~12 MB each)",
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "serving": m["serving"], "serial_single_handles": m["serial_single_handles"],
+        "e2e": m["e2e"], "gpu_launches": m["gpu_launches"], "clocks": m["clocks"],
     }
     return res if rank == 0 else None
 
@@ -543,7 +597,7 @@ def run_precision(args, world, rank, local) -> dict | None:
         "unit": "relative L2 (u, bf16 storage)", "n_gpus": world, "steps": steps, "warmup": 0,
         "ms_per_step": out["f32"]["ms_per_step"], "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32/f16/bf16 vs f64", "data": "synthetic",
-        "config": config_record(base, "precision", {"cells": cells}),
+        "config": dict(config_record(base, "precision", world), cells=cells),
         "variants": out,
     }
     return res if rank == 0 else None
@@ -578,13 +632,127 @@ def run_reference(args, world, rank, local) -> dict | None:
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": el * 1e3 / done, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": config_record(cfg, args.workload, {"parallelism": "host cores"}),
+        "config": config_record(cfg, args.workload, world),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": oracle.oracle_threads(),
                          "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     result["reference_cuda"] = reference_cuda(cfg, args)
+    if args.workload == "default" and not args.no_legs:
+        result["batched"] = reference_batched(args)
+        result["serving"] = reference_serving(args)
+    libs = repo_libraries_mapped()
+    # This arm runs the oracle and the reference's own kernels only: the
+    # library under test must not be mapped into its process.
+    assert not any("libopensayal_gb300" in x for x in libs), libs
+    result["native_libraries"] = libs
     return result
+
+
+def repo_libraries_mapped() -> list[str]:
+    """Shared objects and cubins of this repository mapped into this process."""
+    try:
+        text = Path("/proc/self/maps").read_text()
+    except OSError:
+        return []
+    root = str(ROOT) + "/"
+    out = set()
+    for line in text.splitlines():
+        parts = line.split(None, 5)
+        if len(parts) == 6 and parts[5].startswith(root):
+            out.add(parts[5][len(root):])
+    return sorted(out)
+
+
+def reference_batched(args, sample_every: int = 8, per: int = 2) -> dict:
+    """The batched scenarios (seed 4) one at a time through the reference's own
+    kernels, as its Fluid::update runs them (one launch per sweep, a device
+    synchronisation per step): every `sample_every`-th of the 512 scenarios,
+    one warm step then `per` timed steps each, host wall clock."""
+    import oracle
+    try:
+        import torch
+        if not torch.cuda.is_available() or not oracle.reference_available():
+            return {"unavailable": "no GPU or no reference cubin"}
+        from opensayal_gb300 import scenarios
+        cfgs = scenarios.batched_scenarios(args.scenarios, seed=4)[::sample_every]
+        t, done = 0.0, 0
+        for i, c in enumerate(cfgs):
+            r = oracle.RefFluid(c)
+            u, v = scenarios.perturbation(4000 + i * sample_every, r.is_solid)
+            r.upload("vel_x", u)
+            r.upload("vel_y", v)
+            r.update(None, c.d_t)
+            t0 = time.perf_counter()
+            for _ in range(per):
+                r.update(None, c.d_t)
+            t += time.perf_counter() - t0
+            done += c.width * c.height * per
+            r.close()
+        return {"value": done / t, "unit": UNIT,
+                "workload": BATCHED_WORKLOAD.format(count=args.scenarios),
+                "sample": f"every {sample_every}th scenario ({len(cfgs)} of {args.scenarios}), "
+                          f"{per} steps each after one warm step",
+                "timing": "host wall clock around Fluid::update, which synchronises each step"}
+    except Exception as exc:  # the arm must still print its line
+        return {"unavailable": f"{type(exc).__name__}: {exc}"}
+
+
+def reference_serving(args) -> dict:
+    """The served leg's arrival trace (seed 5) through the reference's own
+    kernels, one request at a time in arrival order (the reference has one
+    Fluid per process and no batching), to the same horizon. Requests that
+    ask for BF16 storage run in FP32: the reference has no other storage."""
+    import oracle
+    try:
+        import torch
+        if not torch.cuda.is_available() or not oracle.reference_available():
+            return {"unavailable": "no GPU or no reference cubin"}
+        from opensayal_gb300 import scenarios
+        from opensayal_gb300.serving import ServeReport
+        reqs = scenarios.serving_requests(args.leg_serve_rate, args.leg_serve_seconds, seed=5)
+        horizon = args.leg_serve_seconds + args.leg_serve_drain
+        warm = oracle.RefFluid(reqs[0].config)
+        warm.update(None, reqs[0].config.d_t)
+        warm.close()
+        rep = ServeReport()
+        t0 = time.perf_counter()
+        for req in reqs:
+            now = time.perf_counter() - t0
+            if now >= horizon:
+                break
+            if req.arrival > now:
+                time.sleep(min(req.arrival - now, horizon - now))
+                if time.perf_counter() - t0 >= horizon:
+                    break
+            rep.arrived += 1
+            rep.admitted += 1
+            rep.offered_cell_steps += req.cells * req.steps
+            c = req.config.copy()
+            c.storage = 0
+            r = oracle.RefFluid(c)
+            u, v = scenarios.perturbation(req.seed, r.is_solid)
+            r.upload("vel_x", u)
+            r.upload("vel_y", v)
+            done = 0
+            while done < req.steps and time.perf_counter() - t0 < horizon:
+                r.update(None, c.d_t)
+                done += 1
+            rep.cell_steps += req.cells * done
+            if done == req.steps:
+                r.download("smoke")
+                rep.latencies_s.append(time.perf_counter() - t0 - req.arrival)
+                rep.finished += 1
+            r.close()
+        rep.wall_s = time.perf_counter() - t0
+        rep.arrived = sum(1 for r in reqs if r.arrival < rep.wall_s)
+        out = rep.summary()
+        return {"value": out["cell_steps_per_s"], "unit": UNIT,
+                "workload": SERVING_WORKLOAD.format(rate=args.leg_serve_rate,
+                                                    seconds=args.leg_serve_seconds),
+                "horizon_s": horizon, "requests": len(reqs), "serial_reference": out}
+    except Exception as exc:  # the arm must still print its line
+        return {"unavailable": f"{type(exc).__name__}: {exc}"}
 
 
 def reference_cuda(cfg, args) -> dict:
@@ -642,6 +810,12 @@ def main():
     ap.add_argument("--serve-slots", type=int, default=64)
     ap.add_argument("--serve-chunk", type=int, default=2)
     ap.add_argument("--no-serial", action="store_true")
+    ap.add_argument("--no-legs", action="store_true",
+                    help="default workload: skip the batched and served legs")
+    ap.add_argument("--leg-serve-rate", type=float, default=1.0,
+                    help="served leg of the default run: Poisson arrivals per second")
+    ap.add_argument("--leg-serve-seconds", type=float, default=20.0)
+    ap.add_argument("--leg-serve-drain", type=float, default=40.0)
     ap.add_argument("--precision-size", type=int, default=0,
                     help="precision: square grid size instead of 4096")
     args = ap.parse_args()

@@ -305,6 +305,22 @@ typedef struct os_arrow {
 } os_arrow;
 
 int os_visual_defaults(os_visual_config* out);
+
+/*
+ * Parses the text of an OpenSayal.conf.json document (`length` bytes, no
+ * terminator needed) as the reference's ConfigParser does: its keys, its
+ * defaults (which follow the parsed sim.width and sim.height), and its
+ * dotted-key lookup (a key is looked up whole first, then split at its first
+ * dot). Fills *cfg (the library's own fields keep os_config_defaults' values)
+ * and, when `visual` is not NULL, *visual. Malformed JSON, or a value of the
+ * wrong type given whole at the top level, is OS_ERR_INVALID (the reference
+ * ends the program); a wrong type inside a nested object yields the default,
+ * as the reference's lookup does. Replaces: ConfigParser::parse()
+ * (src/config_parser.cpp:15-184, inc/config_parser.hpp:131-150); the C++
+ * class ConfigParser in opensayal_gb300/config_parser.hpp reads the file.
+ */
+int os_config_parse(const char* json_text, size_t length, os_config* cfg,
+                    os_visual_config* visual);
 /* W*H RGBA words (r << 24 | g << 16 | b << 8 | a) at y * W + x for pixel
  * (x, y) = (i, H - 1 - j), the cell's own index: solid cells grey, the others
  * coloured by smoke and/or pressure as sim.enable_smoke/enable_pressure say

@@ -25,6 +25,7 @@
 #include <string>
 
 #include "../opensayal_gb300.h"
+#include "config_parser.hpp"
 
 // --- inc/helper.cuh:7-75 ---------------------------------------------------
 template <typename T>
@@ -42,35 +43,6 @@ class Vector2d {
   T y_;
 };
 
-// --- inc/config_parser.hpp:9-116 -------------------------------------------
-struct ColorConfig { int r; int g; int b; int a; };
-struct OpenMPConfig { int thread_count; };
-struct CudaConfig { int block_size_x; int block_size_y; };
-struct ThreadConfig { OpenMPConfig openMP; CudaConfig cuda; };
-struct ProjectionConfig { int n; float o; };
-struct PhysicsConfig { float g; };
-struct WindTunnelConfig {
-  int pipe_height; int pipe_length; int smoke_length; int smoke_height; int smoke_count;
-  float speed; float smoke;
-};
-struct ObstacleConfig { bool enable; int center_x; int center_y; float radius; };
-struct TimeConfig { float d_t; bool enable_real_time; float real_time_multiplier; };
-struct SmokeConfig { bool enable_decay; float decay_rate; };
-struct PathLineConfig { bool enable; int length; ColorConfig color; int distance; };
-struct FluidConfig { float density; float drag_coeff; float viscosity; };
-struct SimConfig {
-  int height; int width; int cell_pixel_size; float cell_size;
-  bool enable_drain; bool enable_pressure; bool enable_smoke; bool enable_interactive;
-  ProjectionConfig projection; WindTunnelConfig wind_tunnel; PhysicsConfig physics;
-  TimeConfig time; SmokeConfig smoke; ObstacleConfig obstacle;
-};
-struct ArrowConfig {
-  ColorConfig color; bool enable; int distance; float length_multiplier;
-  float disable_threshold; int head_length;
-};
-struct VisualConfig { ArrowConfig arrows; PathLineConfig path_line; };
-struct Config { ThreadConfig thread; SimConfig sim; FluidConfig fluid; VisualConfig visual; };
-
 // --- inc/fluid.cuh:8-13 -----------------------------------------------------
 struct Source {
   bool active;
@@ -81,54 +53,9 @@ struct Source {
 
 namespace opensayal {
 
-struct Error : std::runtime_error {
-  int code;
-  Error(int c, const std::string& what) : std::runtime_error(what), code(c) {}
-};
-
-inline void check(int rc) {
-  if (rc != OS_OK) throw Error(rc, os_last_error());
-}
-
-// Config -> os_config (every key the simulation reads).
-inline os_config to_os_config(const Config& c) {
-  os_config o;
-  check(os_config_defaults(c.sim.width, c.sim.height, &o));
-  o.block_size_x = c.thread.cuda.block_size_x;
-  o.block_size_y = c.thread.cuda.block_size_y;
-  o.cell_pixel_size = c.sim.cell_pixel_size;
-  o.cell_size = c.sim.cell_size;
-  o.enable_drain = c.sim.enable_drain;
-  o.enable_pressure = c.sim.enable_pressure;
-  o.enable_smoke = c.sim.enable_smoke;
-  o.enable_interactive = c.sim.enable_interactive;
-  o.projection_n = c.sim.projection.n;
-  o.projection_o = c.sim.projection.o;
-  o.pipe_height = c.sim.wind_tunnel.pipe_height;
-  o.pipe_length = c.sim.wind_tunnel.pipe_length;
-  o.smoke_length = c.sim.wind_tunnel.smoke_length;
-  o.smoke_height = c.sim.wind_tunnel.smoke_height;
-  o.smoke_count = c.sim.wind_tunnel.smoke_count;
-  o.tunnel_speed = c.sim.wind_tunnel.speed;
-  o.tunnel_smoke = c.sim.wind_tunnel.smoke;
-  o.g = c.sim.physics.g;
-  o.d_t = c.sim.time.d_t;
-  o.enable_real_time = c.sim.time.enable_real_time;
-  o.real_time_multiplier = c.sim.time.real_time_multiplier;
-  o.smoke_enable_decay = c.sim.smoke.enable_decay;
-  o.smoke_decay_rate = c.sim.smoke.decay_rate;
-  o.obstacle_enable = c.sim.obstacle.enable;
-  o.obstacle_center_x = c.sim.obstacle.center_x;
-  o.obstacle_center_y = c.sim.obstacle.center_y;
-  o.obstacle_radius = c.sim.obstacle.radius;
-  o.density = c.fluid.density;
-  o.drag_coeff = c.fluid.drag_coeff;
-  o.viscosity = c.fluid.viscosity;
-  return o;
-}
-
 inline os_handle* create(const Config& c) {
-  os_config o = to_os_config(c);
+  os_config o;
+  check(to_os_config(c, &o));
   os_handle* h = nullptr;
   check(os_create(&o, &h));
   return h;

@@ -1,4 +1,4 @@
-"""In-tree build of the CUDA library (sm_103a) and of the test-only checkers.
+"""In-tree build of the CUDA library (sm_103a).
 
 `build_library()` compiles opensayal_gb300/csrc into
 opensayal_gb300/lib/libopensayal_gb300.so with nvcc, for GB300 only
@@ -65,23 +65,6 @@ def build_library(force: bool = False, verbose: bool = False) -> Path:
         print(res.stderr)
     os.replace(tmp, LIB_PATH)
     return LIB_PATH
-
-
-def build_checkers(with_reference: bool | None = None) -> None:
-    """Build oracle/ (test infrastructure): the C restatement, the harness for
-    the reference's kernels and, where the reference sources are present, the
-    reference cubin."""
-    oracle = ROOT / "oracle"
-    targets = ["all"]
-    ref_src = Path(os.environ.get("OPENSAYAL_REFERENCE", "/root/reference"))
-    if with_reference is None:
-        with_reference = (ref_src / "src" / "fluid.cu").exists()
-    if with_reference:
-        targets.append("ref")
-    res = subprocess.run(["make", "-s", "-C", str(oracle), *targets,
-                          f"REFERENCE={ref_src}"], capture_output=True, text=True)
-    if res.returncode != 0:
-        raise RuntimeError(f"oracle build failed:\n{res.stdout}\n{res.stderr}")
 
 
 if __name__ == "__main__":

@@ -26,6 +26,7 @@
 #include <vector>
 
 #include "../../include/opensayal_gb300.h"
+#include "../../include/opensayal_gb300/config_parser.hpp"
 #include "os_kernels.cuh"
 
 using namespace osg;
@@ -1109,6 +1110,21 @@ int os_visual_defaults(os_visual_config* out) {
   return OS_OK;
 }
 
+int os_config_parse(const char* json_text, size_t length, os_config* cfg,
+                    os_visual_config* visual) {
+  if (!json_text || !cfg) return set_err(OS_ERR_INVALID, "null argument");
+  try {
+    const Config c =
+        opensayal::config_from_json(opensayal::json::parse(std::string(json_text, length)));
+    int rc = opensayal::to_os_config(c, cfg);
+    if (rc != OS_OK) return rc;
+    if (visual) opensayal::to_os_visual_config(c, visual);
+  } catch (const std::exception& e) {
+    return set_err(OS_ERR_INVALID, "config: %s", e.what());
+  }
+  return OS_OK;
+}
+
 static int visual_params(const os_handle* h, const os_visual_config* v, VisualParams* vp) {
   if (!v) return set_err(OS_ERR_INVALID, "null visual config");
   if (v->cell_pixel_size < 1 || v->arrow_distance < 1 || v->trace_distance < 1 ||
@@ -1476,7 +1492,8 @@ int noalloc_scratch(int device, float** out) {
   return OS_OK;
 }
 
-// k_diffuse's sweep with dt passed by value (no device parameter block).
+// k_diffuse's sweep (the same diffuse_cell) with dt passed by value, so no
+// device parameter block is needed.
 __global__ void k_diffuse_noalloc(const float* __restrict__ uin, float* __restrict__ uout,
                                   Consts c, float d_t) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1488,9 +1505,7 @@ __global__ void k_diffuse_noalloc(const float* __restrict__ uin, float* __restri
     uout[k] = uin[k];
     return;
   }
-  float a = c.viscosity * d_t / (float)(c.h * c.h);
-  float val = (uin[k] + a * (uin[k - 1] + uin[k + 1] + uin[k + W] + uin[k - W])) / (1 + 4 * a);
-  uout[k] = val;
+  diffuse_cell<float, float>(uin, uout, k, W, diffusion_coeff<float>(c, d_t));
 }
 
 }  // namespace

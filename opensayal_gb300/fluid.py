@@ -35,9 +35,36 @@ class Source:
 
 
 def default_config(width: int = 1920, height: int = 1080) -> OsConfig:
-    """ConfigParser defaults for a width x height tunnel (src/config_parser.cpp:21-179)."""
-    cfg = OsConfig()
-    check(native.load().os_config_defaults(width, height, C.byref(cfg)))
+    """ConfigParser defaults for a width x height tunnel (src/config_parser.cpp:21-179).
+
+    Filled in here, without loading the CUDA library, so that configurations
+    can be built where the library is absent or must not be mapped (the CPU
+    checkers). The C ABI's os_config_defaults gives the same structure, field
+    for field (tests/test_abi.py compares the two)."""
+    if width < 1 or height < 1:
+        raise ValueError(f"bad size {width}x{height}")
+    cfg = OsConfig()  # zero-filled: storage F32, device 0, autotuned depths
+    cfg.block_size_x, cfg.block_size_y = 64, 1
+    cfg.height, cfg.width = height, width
+    cfg.cell_pixel_size = 1
+    cfg.cell_size = 1.0
+    cfg.enable_drain, cfg.enable_pressure, cfg.enable_smoke, cfg.enable_interactive = 1, 0, 1, 0
+    cfg.projection_n, cfg.projection_o = 50, 1.9
+    cfg.pipe_height = height // 4
+    cfg.pipe_length = 0  # hard-coded by the parser (src/config_parser.cpp:64)
+    cfg.smoke_length = 1
+    cfg.smoke_height = height // 4
+    cfg.smoke_count = 1
+    cfg.tunnel_speed, cfg.tunnel_smoke = 0.0, 1.0
+    cfg.g = 0.0
+    cfg.d_t = 0.05
+    cfg.enable_real_time, cfg.real_time_multiplier = 0, 1.0
+    cfg.smoke_enable_decay, cfg.smoke_decay_rate = 0, 0.05
+    cfg.obstacle_enable = 1
+    cfg.obstacle_center_x, cfg.obstacle_center_y = width // 2, height // 2
+    # std::min(height, width) / 30.0f: an FP32 division
+    cfg.obstacle_radius = float(np.float32(min(height, width)) / np.float32(30.0))
+    cfg.density, cfg.drag_coeff, cfg.viscosity = 1.0, 0.0, 0.001
     return cfg
 
 
@@ -76,58 +103,73 @@ CONFIG_KEYS: dict[str, tuple[str, type]] = {
     "fluid.viscosity": ("viscosity", float),
 }
 
-_MISSING = object()
-
-
-def _get_or(obj: Any, key: str) -> Any:
-    """ConfigParser::get_or (inc/config_parser.hpp:131-150): the whole dotted key
-    at this level first, then recurse on the part before the first dot."""
-    if isinstance(obj, dict) and key in obj:
-        return obj[key]
-    if key == "" or "." not in key:
-        return _MISSING
-    parent, child = key.split(".", 1)
-    if not isinstance(obj, dict) or parent not in obj:
-        return _MISSING
-    return _get_or(obj[parent], child)
+class _WrongType(TypeError):
+    pass
 
 
 def _convert(value: Any, typ: type, key: str) -> Any:
+    """The conversions of the reference's JSON library: a boolean key needs a
+    JSON boolean; numbers (and booleans) convert to int by truncation and to
+    float by rounding."""
     if typ is bool:
         if not isinstance(value, bool):
-            raise TypeError(f"config key {key!r} must be a boolean, got {value!r}")
+            raise _WrongType(f"config key {key!r} must be a boolean, got {value!r}")
         return int(value)
-    if isinstance(value, bool) or not isinstance(value, (int, float)):
-        raise TypeError(f"config key {key!r} must be a number, got {value!r}")
+    if not isinstance(value, (bool, int, float)):
+        raise _WrongType(f"config key {key!r} must be a number, got {value!r}")
     return int(value) if typ is int else float(value)
+
+
+def _get_or(obj: Any, key: str, typ: type, default: Any, top: bool = True) -> Any:
+    """ConfigParser::get_or (inc/config_parser.hpp:131-150): the whole dotted key
+    at this level first, then recurse on the part after the first dot inside
+    the member named by the part before it. A wrong type found below the top
+    level yields the default (the reference's catch-all around the
+    recursion); at the top level it is an error."""
+    if isinstance(obj, dict) and key in obj:
+        try:
+            return _convert(obj[key], typ, key)
+        except _WrongType:
+            if top:
+                raise
+            return default
+    if key == "" or "." not in key:
+        return default
+    parent, child = key.split(".", 1)
+    if not isinstance(obj, dict) or parent not in obj:
+        return default
+    return _get_or(obj[parent], child, typ, default, top=False)
 
 
 def visual_defaults() -> native.OsVisualConfig:
     """The `visual.*` and `sim.cell_pixel_size` defaults of
     src/config_parser.cpp:39-40, 120-179."""
     v = native.OsVisualConfig()
-    check(native.load().os_visual_defaults(C.byref(v)))
+    v.cell_pixel_size = 1
+    v.arrow_distance = 20
+    v.arrow_length_multiplier = 0.1
+    v.arrow_disable_threshold = 0.0
+    v.arrow_head_length = 5
+    v.trace_distance = 20
+    v.trace_length = 20
     return v
 
 
 def load_config(source: dict | str | Path) -> OsConfig:
-    """Parse an OpenSayal.conf.json (path, JSON text or dict) with the reference's
+    """Parse an OpenSayal.conf.json (a path, JSON text or a dict) with the reference's
     defaults and dotted-key lookup. Size-dependent defaults (pipe and smoke
     heights, obstacle centre and radius) follow the parsed width and height."""
     if isinstance(source, dict):
         obj = source
+    elif isinstance(source, Path) or not str(source).lstrip().startswith(("{", "[")):
+        obj = json.loads(Path(source).read_text())
     else:
-        text = Path(source).read_text() if Path(str(source)).exists() else str(source)
-        obj = json.loads(text)
-    width = _get_or(obj, "sim.width")
-    height = _get_or(obj, "sim.height")
-    width = 1920 if width is _MISSING else _convert(width, int, "sim.width")
-    height = 1080 if height is _MISSING else _convert(height, int, "sim.height")
+        obj = json.loads(source)
+    width = _get_or(obj, "sim.width", int, 1920)
+    height = _get_or(obj, "sim.height", int, 1080)
     cfg = default_config(width, height)
     for key, (field, typ) in CONFIG_KEYS.items():
-        val = _get_or(obj, key)
-        if val is not _MISSING:
-            setattr(cfg, field, _convert(val, typ, key))
+        setattr(cfg, field, _get_or(obj, key, typ, getattr(cfg, field)))
     return cfg
 
 

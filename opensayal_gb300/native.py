@@ -130,6 +130,7 @@ SIGNATURES = [
     ("os_diffuse_noalloc", C.c_int, [C.POINTER(OsConfig), C.c_void_p, C.c_float, C.c_void_p]),
     ("os_diagnose", C.c_int, [C.c_void_p, C.c_void_p]),
     ("os_visual_defaults", C.c_int, [C.c_void_p]),
+    ("os_config_parse", C.c_int, [C.c_char_p, C.c_size_t, C.POINTER(OsConfig), C.c_void_p]),
     ("os_render_pixels", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     ("os_render_arrows", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("os_render_traces", C.c_int, [C.c_void_p, C.c_void_p, C.c_float, C.c_void_p, C.c_void_p,

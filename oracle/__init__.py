@@ -28,8 +28,24 @@ def reference_diffusion_sweeps(n: int) -> int:
     return n
 
 
-def build() -> None:
-    res = subprocess.run(["make", "-s", "-C", str(HERE), "all"], capture_output=True, text=True)
+def build(with_reference: bool | None = None) -> None:
+    """Build the checkers with oracle/Makefile: the C restatement, the harness
+    for the reference's kernels and, where the reference sources are present
+    (the Makefile's REFERENCE, overridable with OPENSAYAL_REFERENCE), the
+    reference cubins. Elsewhere the cubins already in _ref/ are used."""
+    targets = ["all"]
+    env_ref = os.environ.get("OPENSAYAL_REFERENCE")
+    if with_reference is None:
+        probe = subprocess.run(["make", "-s", "-C", str(HERE), "--no-print-directory",
+                                "print-reference"] + ([f"REFERENCE={env_ref}"] if env_ref else []),
+                               capture_output=True, text=True)
+        ref_dir = Path(probe.stdout.strip() or "/nonexistent")
+        with_reference = (ref_dir / "src" / "fluid.cu").exists()
+    if with_reference:
+        targets.append("ref")
+    extra = [f"REFERENCE={env_ref}"] if env_ref else []
+    res = subprocess.run(["make", "-s", "-C", str(HERE), *targets, *extra],
+                         capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"oracle build failed:\n{res.stdout}\n{res.stderr}")
 

@@ -4,6 +4,7 @@ follows the reference's ConfigParser."""
 import ctypes as C
 import re
 import subprocess
+import sys
 
 import numpy as np
 import pytest
@@ -103,6 +104,31 @@ def test_defaults_follow_config_parser(lib_built):
     assert c.storage == 0 and c.idw_mode == 0
 
 
+@pytest.mark.parametrize("size", [(1920, 1080), (256, 128), (4096, 4096), (97, 250), (7, 3),
+                                  (1000, 330), (1, 1)])
+def test_python_defaults_equal_the_c_abi_defaults(lib_built, size):
+    """default_config is filled in Python (no library load); it must equal
+    os_config_defaults byte for byte, and so must visual_defaults."""
+    from opensayal_gb300.fluid import visual_defaults
+    lib = native.load()
+    c = native.OsConfig()
+    assert lib.os_config_defaults(size[0], size[1], C.byref(c)) == native.OS_OK
+    py = default_config(*size)
+    assert bytes(py) == bytes(c), (py.as_dict(), c.as_dict())
+    v = native.OsVisualConfig()
+    assert lib.os_visual_defaults(C.byref(v)) == native.OS_OK
+    assert bytes(visual_defaults()) == bytes(v)
+
+
+def test_default_config_does_not_load_the_library():
+    code = ("import sys; sys.path.insert(0, %r)\n"
+            "from opensayal_gb300 import scenarios\n"
+            "scenarios.default_tunnel_config(); scenarios.batched_scenarios(4)\n"
+            "maps = open('/proc/self/maps').read()\n"
+            "assert 'libopensayal_gb300' not in maps, 'library mapped'\n" % str(ROOT))
+    subprocess.run([sys.executable, "-c", code], check=True)
+
+
 def test_load_config_dotted_and_nested_keys(lib_built):
     """ConfigParser::get_or (inc/config_parser.hpp:131-150): a dotted key may be
     given whole at any level or as nested objects; absent keys take defaults that
@@ -119,8 +145,12 @@ def test_load_config_dotted_and_nested_keys(lib_built):
     cfg2 = load_config('{"sim.width": 300, "sim": {"height": 90}}')
     assert (cfg2.width, cfg2.height) == (300, 90)
     assert cfg2.obstacle_radius == np.float32(90 / 30.0)
+    # A wrong type inside a nested object yields the default (the reference's
+    # catch-all around its recursion); given whole at the top level it is an error.
+    assert load_config({"sim": {"enable_drain": 1}}).enable_drain == 1
+    assert load_config({"sim": {"enable_drain": False, "width": "wide"}}).width == 1920
     with pytest.raises(TypeError):
-        load_config({"sim": {"enable_drain": 1}})
+        load_config({"sim.enable_drain": 1})
     assert len(CONFIG_KEYS) == 31
 
 

@@ -16,6 +16,9 @@ EXE = ROOT / "oracle" / "build" / "drop_in_main"
 
 
 def build_program():
+    deps = [SRC, *(ROOT / "include").rglob("*.h*"), LIB_DIR / "libopensayal_gb300.so"]
+    if EXE.exists() and all(d.stat().st_mtime <= EXE.stat().st_mtime for d in deps):
+        return EXE
     EXE.parent.mkdir(parents=True, exist_ok=True)
     cmd = ["g++", "-std=c++17", "-O2", f"-I{ROOT / 'include'}", "-I/usr/local/cuda/include",
            str(SRC), "-o", str(EXE), f"-L{LIB_DIR}", "-lopensayal_gb300",

@@ -50,10 +50,11 @@ def via_noalloc(cfg, u0, dt):
     return dev.cpu().numpy()
 
 
-@pytest.mark.parametrize("n", [7, 8])
-def test_noalloc_diffusion_equals_handle_diffusion_twice(gpu, n):
+@pytest.mark.parametrize("w,h,n", [(300, 161, 7), (300, 161, 8),
+                                   (1024, 1024, 5)])  # the largest grid it accepts, odd n
+def test_noalloc_diffusion_equals_handle_diffusion_twice(gpu, w, h, n):
     rng = np.random.default_rng(n)
-    cfg = tunnel(300, 161, n)
+    cfg = tunnel(w, h, n)
     for call in range(2):  # the second call starts from the first call's leftovers
         u0 = rng.uniform(-2, 2, cfg.width * cfg.height).astype(np.float32)
         want = via_handle(cfg, u0, 0.05)
