@@ -51,6 +51,29 @@ def peaks() -> dict:
     return {"hbm_gbs": FALLBACK_HBM_GBS, "source": "fallback"}
 
 
+def l2_copy_peak(device: int) -> dict:
+    """The L2 copy bandwidth, measured live: the library's bandwidth probe
+    (one launch copying a buffer back and forth `reps` times with
+    cache-at-L2 loads and stores) on buffers whose pair fits in the 129 MB
+    L2; the best of three runs per size is kept. The stencil phases keep
+    their sweeps on the SM and exchange through L2, so this is the level
+    their effective rate is compared with."""
+    import ctypes as C
+    from opensayal_gb300 import native
+    lib = native.load()
+    best = {"gbs": 0.0}
+    for mib in (8, 16, 24):
+        for _ in range(3):
+            g = C.c_float()
+            native.check(lib.os_probe_copy_bandwidth(device, mib << 20, 200, C.byref(g)))
+            if g.value > best["gbs"]:
+                best = {"gbs": float(g.value), "buffer_mib": mib}
+    best["how"] = ("os_probe_copy_bandwidth: two buffers of 8-24 MiB copied back and forth 200 "
+                   "times in one launch (ld/st.global.cg), read+write bytes / CUDA-event time, "
+                   "best of 3 per size")
+    return best
+
+
 def bytes_per_cell_step(n: int, viscous: bool) -> int:
     """Compulsory FP32 traffic of an unfused phase-per-pass schedule (1-byte
     flags): forces 8, diffusion 8/sweep, projection 17/sweep, advection 17+17."""
@@ -300,6 +323,7 @@ def run_gb300(args, world, rank, local) -> dict | None:
             ":resident" if f.fields().projection_resident else "")
         traffic = json.loads(tfile.read_text()).get(key)
     step_bytes = bytes_per_cell_step(cfg.projection_n, cfg.viscosity != 0.0)
+    l2 = l2_copy_peak(local)
     ms_per_step = total_s * 1e3 / args.steps
     result = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
@@ -317,6 +341,13 @@ def run_gb300(args, world, rank, local) -> dict | None:
                      "unit": "GB/s", "frac": achieved / pk["hbm_gbs"], "traffic": traffic,
                      "kernel": "projection phase (17 B/cell per red/black sweep x n sweeps)",
                      "launches": proj_kernels // 3, "peak_source": pk["source"]},
+        # The projection's sweeps run in shared memory and its halo exchanges
+        # go through L2; DRAM sees the fields about once per phase. The level
+        # that binds is on-chip, so the same algorithmic rate is also given
+        # against a live L2-resident copy.
+        "roofline_l2": {"bound": "l2", "achieved": achieved, "peak": l2["gbs"], "unit": "GB/s",
+                        "frac": achieved / l2["gbs"], "peak_source": "measured live: " + l2["how"],
+                        "peak_buffer_mib": l2.get("buffer_mib")},
         "step_roofline": {"bytes_per_cell_step": step_bytes,
                           "achieved": step_bytes * value / world / 1e9, "unit": "GB/s",
                           "frac": step_bytes * value / world / 1e9 / pk["hbm_gbs"]},
@@ -337,8 +368,10 @@ def run_gb300(args, world, rank, local) -> dict | None:
                                             args.warmup, baselines=not args.no_cpu_baseline)
         result["serving"] = serving_measure(world, rank, local, args.leg_serve_rate,
                                             args.leg_serve_seconds, args.leg_serve_drain,
-                                            args.serve_budget_gb, args.serve_slots,
-                                            args.serve_chunk, serial=not args.no_serial)
+                                            args.serve_budget_gb, args.serve_slots or None,
+                                            args.serve_chunk, serial=not args.no_serial,
+                                            lanes=args.serve_lanes,
+                                            saturation_mcells=args.serve_saturation_mcells or None)
     return result if rank == 0 else None
 
 
@@ -470,7 +503,8 @@ SERVING_WORKLOAD = ("serving: Poisson {rate:g}/s for {seconds:g} s (seed 5), tun
 
 
 def serving_measure(world, rank, local, rate: float, seconds: float, drain: float,
-                    budget_gb: float, slots: int, chunk: int, serial: bool = True) -> dict:
+                    budget_gb: float, slots: int | None, chunk: int, serial: bool = True,
+                    lanes: int = 4, saturation_mcells: float | None = 48.0) -> dict:
     """Poisson arrivals (seed 5) of tunnels drawn as in the batched workload,
     steps U[100, 5000], BF16 or FP32 storage (p = 0.5), served by continuous
     batching within a device-memory budget; the same arrival trace served one
@@ -492,12 +526,14 @@ def serving_measure(world, rank, local, rate: float, seconds: float, drain: floa
     for r in warm:
         r.config.device = local
         r.steps = 3
-    with Server(budget_bytes=1 << 30, block_k=8, max_members=2) as w:
+    with Server(budget_bytes=1 << 30, block_k=8, max_members=2, lanes=1) as w:
         w.run(warm, 60.0)
     budget = int(budget_gb * 1e9)
+    sat = int(saturation_mcells * 1e6) if saturation_mcells else None
     dist_barrier(world)
     with Clocks(local) as clk:
-        with Server(budget_bytes=budget, block_k=8, max_members=slots, chunk=chunk) as srv:
+        with Server(budget_bytes=budget, block_k=8, max_members=slots, chunk=chunk, lanes=lanes,
+                    saturation_cells=sat) as srv:
             rep = srv.run(reqs, horizon)
             st = srv.batch.stats()
     served = rep.summary()
@@ -506,7 +542,8 @@ def serving_measure(world, rank, local, rate: float, seconds: float, drain: floa
     return {
         "value": value, "unit": UNIT,
         "workload": SERVING_WORKLOAD.format(rate=rate, seconds=seconds),
-        "budget_gb": budget_gb, "max_members": slots, "chunk": chunk, "horizon_s": horizon,
+        "budget_gb": budget_gb, "max_members": slots, "lanes": lanes,
+        "saturation_mcells": saturation_mcells, "chunk": chunk, "horizon_s": horizon,
         "block_k": st.block_k, "requests": len(reqs),
         "serving": served, "serial_single_handles": serial_rep,
         "e2e": {"value": value, "unit": UNIT,
@@ -520,8 +557,9 @@ def serving_measure(world, rank, local, rate: float, seconds: float, drain: floa
 def run_serving(args, world, rank, local) -> dict | None:
     """The served scenarios as the line's own workload (--workload serving)."""
     m = serving_measure(world, rank, local, args.serve_rate, args.serve_seconds,
-                        args.serve_drain, args.serve_budget_gb, args.serve_slots,
-                        args.serve_chunk, serial=not args.no_serial)
+                        args.serve_drain, args.serve_budget_gb, args.serve_slots or None,
+                        args.serve_chunk, serial=not args.no_serial, lanes=args.serve_lanes,
+                        saturation_mcells=args.serve_saturation_mcells or None)
     steps = max(1, m["steps_enqueued"])
     res = {
         "metric": "served cell-steps/s (continuous batching, Poisson arrivals)",
@@ -530,7 +568,8 @@ def run_serving(args, world, rank, local) -> dict | None:
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32/bf16",
         "data": "synthetic",
         "config": {"workload": m["workload"], "budget_gb": m["budget_gb"],
-                   "max_members": m["max_members"], "chunk": m["chunk"],
+                   "max_members": m["max_members"], "lanes": m["lanes"],
+                   "saturation_mcells": m["saturation_mcells"], "chunk": m["chunk"],
                    "horizon_s": m["horizon_s"],
                    "l2": "inputs larger than L2 (tens of members, ~12 MB each)",
                    "parallelism": "replicas" if world > 1 else "single"},
@@ -542,25 +581,30 @@ def run_serving(args, world, rank, local) -> dict | None:
 
 def run_precision(args, world, rank, local) -> dict | None:
     """Storage precision against an FP64 run of the same scheme: the 4096x4096
-    tunnel (n = 200, dt = 0.02) from the same seeded state, `--steps` steps in
-    FP32, FP16 and BF16 storage (FP32 arithmetic) and in FP64 storage and
-    arithmetic; per-field relative L2 against FP64 and the FP64 diagnostics of
-    every run. The workload can be scaled down with --precision-size."""
+    tunnel (n = 200, dt = 0.02) from the same seeded state, in FP32, FP16 and
+    BF16 storage (FP32 arithmetic) and in FP64 storage and arithmetic; the
+    per-field relative L2 against FP64 at every checkpoint of
+    `--precision-steps` (cumulative step counts), and the FP64 diagnostics of
+    every run at the last one. The grid can be scaled down with
+    --precision-size (256 gives the 256x128-shaped small tunnel)."""
     import torch
     from opensayal_gb300 import Fluid, scenarios
     from opensayal_gb300.build import build_library
     build_library()
     torch.cuda.set_device(local)
-    base = scenarios.large_config()
-    if args.precision_size:
-        s = args.precision_size / base.width
-        base.width = base.height = args.precision_size
-        base.pipe_height = int(base.pipe_height * s)
-        base.obstacle_center_x = base.obstacle_center_y = args.precision_size // 2
-        base.obstacle_radius = base.obstacle_radius * s
-        base.smoke_height = base.height // 4
+    if args.precision_size == 256:
+        base = scenarios.small_config()
+    else:
+        base = scenarios.large_config()
+        if args.precision_size:
+            sc = args.precision_size / base.width
+            base.width = base.height = args.precision_size
+            base.pipe_height = int(base.pipe_height * sc)
+            base.obstacle_center_x = base.obstacle_center_y = args.precision_size // 2
+            base.obstacle_radius = base.obstacle_radius * sc
+            base.smoke_height = base.height // 4
     base.device = local
-    steps = args.steps
+    checkpoints = sorted({int(x) for x in str(args.precision_steps).split(",") if x})
     fields = ("vel_x", "vel_y", "smoke")
     runs = {}
     for name, storage in (("f64", 3), ("f32", 0), ("f16", 1), ("bf16", 2)):
@@ -570,34 +614,47 @@ def run_precision(args, world, rank, local) -> dict | None:
         u, v = scenarios.perturbation(3, f.download("is_solid"))
         f.upload("vel_x", u)
         f.upload("vel_y", v)
-        t0 = time.perf_counter()
-        f.update_async(None, cfg.d_t, steps)
-        f.synchronize()
-        elapsed = time.perf_counter() - t0
-        runs[name] = {"fields": {k: f.download(k).astype(np.float64) for k in fields},
-                      "diag": f.diagnose(), "ms_per_step": elapsed * 1e3 / steps,
-                      "projection_block": f.fields().projection_block}
+        snaps, done, elapsed = {}, 0, 0.0
+        for cp in checkpoints:
+            t0 = time.perf_counter()
+            f.update_async(None, cfg.d_t, cp - done)
+            f.synchronize()
+            elapsed += time.perf_counter() - t0
+            done = cp
+            snaps[cp] = {k: f.download(k).astype(np.float64) for k in fields}
+        runs[name] = {"snaps": snaps, "diag": f.diagnose(), "ms_per_step": elapsed * 1e3 / done,
+                      "projection_block": f.fields().projection_block,
+                      "projection_resident": f.fields().projection_resident}
         f.close()
     ref = runs["f64"]
     out = {}
     for name, r in runs.items():
-        rel = {}
-        for k in fields:
-            den = float(np.linalg.norm(ref["fields"][k])) or 1.0
-            rel[k] = float(np.linalg.norm(r["fields"][k] - ref["fields"][k])) / den
+        curve = {}
+        for cp in checkpoints:
+            rel = {}
+            for k in fields:
+                want = ref["snaps"][cp][k]
+                den = float(np.linalg.norm(want)) or 1.0
+                rel[k] = float(np.linalg.norm(r["snaps"][cp][k] - want)) / den
+            curve[str(cp)] = rel
         dr = {}
         for k in ("divergence_l2", "smoke_mass", "inflow_flux", "outflow_flux"):
             den = abs(ref["diag"][k]) or 1.0
             dr[k] = abs(r["diag"][k] - ref["diag"][k]) / den
-        out[name] = {"rel_l2_vs_f64": rel, "diag": r["diag"], "diag_rel_err_vs_f64": dr,
-                     "ms_per_step": r["ms_per_step"], "projection_block": r["projection_block"]}
+        out[name] = {"rel_l2_vs_f64": curve, "diag": r["diag"], "diag_rel_err_vs_f64": dr,
+                     "ms_per_step": r["ms_per_step"], "projection_block": r["projection_block"],
+                     "projection_resident": r["projection_resident"]}
+    last = str(checkpoints[-1])
     cells = base.width * base.height
     res = {
-        "metric": "relative L2 vs FP64 run of the same scheme", "value": out["bf16"]["rel_l2_vs_f64"]["vel_x"],
-        "unit": "relative L2 (u, bf16 storage)", "n_gpus": world, "steps": steps, "warmup": 0,
+        "metric": "relative L2 vs FP64 run of the same scheme",
+        "value": out["bf16"]["rel_l2_vs_f64"][last]["vel_x"],
+        "unit": "relative L2 (u, bf16 storage, last checkpoint)", "n_gpus": world,
+        "steps": checkpoints[-1], "warmup": 0,
         "ms_per_step": out["f32"]["ms_per_step"], "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32/f16/bf16 vs f64", "data": "synthetic",
-        "config": dict(config_record(base, "precision", world), cells=cells),
+        "config": dict(config_record(base, "precision", world), cells=cells,
+                       checkpoints=checkpoints),
         "variants": out,
     }
     return res if rank == 0 else None
@@ -807,7 +864,12 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=60.0)
     ap.add_argument("--serve-drain", type=float, default=30.0)
     ap.add_argument("--serve-budget-gb", type=float, default=150.0)
-    ap.add_argument("--serve-slots", type=int, default=64)
+    ap.add_argument("--serve-slots", type=int, default=0,
+                    help="members the batch may hold (0: bounded by memory and saturation)")
+    ap.add_argument("--serve-lanes", type=int, default=4,
+                    help="latency lanes: requests run on single handles of their own")
+    ap.add_argument("--serve-saturation-mcells", type=float, default=48.0,
+                    help="cells (millions) the batch holds at most (0: memory only)")
     ap.add_argument("--serve-chunk", type=int, default=2)
     ap.add_argument("--no-serial", action="store_true")
     ap.add_argument("--no-legs", action="store_true",
@@ -817,7 +879,9 @@ def main():
     ap.add_argument("--leg-serve-seconds", type=float, default=20.0)
     ap.add_argument("--leg-serve-drain", type=float, default=40.0)
     ap.add_argument("--precision-size", type=int, default=0,
-                    help="precision: square grid size instead of 4096")
+                    help="precision: square grid size instead of 4096 (256: the small tunnel)")
+    ap.add_argument("--precision-steps", default="100,250,500,1000",
+                    help="precision: cumulative step counts at which the errors are taken")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

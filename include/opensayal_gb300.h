@@ -212,6 +212,10 @@ int os_update_async(os_handle* h, const os_source* src, float dt,
 
 /* Waits for all work enqueued on the handle's stream. */
 int os_synchronize(os_handle* h);
+/* Without waiting: *idle = 1 when everything enqueued on the handle's own
+ * stream has completed (and the resident waits reported no failure), else 0.
+ * No reference counterpart (the reference's update always synchronises). */
+int os_query(os_handle* h, int32_t* idle);
 
 /* Device pointers of the public fields. Replaces: reading Fluid::d_* members. */
 int os_fields(os_handle* h, os_fields_view* out);
@@ -347,6 +351,16 @@ int os_render_traces(os_handle* h, const os_visual_config* v, float dt, int32_t*
  * counterpart.
  */
 int os_selftest_bounded_wait(int32_t device, int32_t* status);
+
+/*
+ * Copy bandwidth probe for rooflines (no reference counterpart): allocates
+ * two buffers of `bytes` (a positive multiple of 16) on `device`, copies one
+ * into the other `reps` times in one launch with cache-at-L2 loads and
+ * stores, alternating direction, and reports read + write bytes per second
+ * of the timed launch in *gbs (GB/s, 1e9). Buffers that together fit in L2
+ * measure the L2 copy bandwidth; larger ones measure HBM.
+ */
+int os_probe_copy_bandwidth(int32_t device, uint64_t bytes, int32_t reps, float* gbs);
 
 /*
  * FP64 diagnostics of the current fields (no reference counterpart). The

@@ -76,4 +76,12 @@ __host__ __device__ __forceinline__ int64_t cell_index(int W, int H, int i, int 
   return (int64_t)(H - 1 - j) * W + i;
 }
 
+// The same index in 32 bits, for the gathers of the advection kernels: a
+// grid, with its one-cell ring, has fewer than 2^31 cells (the reference's
+// own indices are int, and os_create refuses larger grids), so every index
+// and offset fits, and each address is one 32 x 64-bit multiply-add.
+__host__ __device__ __forceinline__ int cell_index32(int W, int H, int i, int j) {
+  return (H - 1 - j) * W + i;
+}
+
 }  // namespace osg

@@ -569,8 +569,11 @@ int push_params(os_handle* h, const os_source* src, float dt, cudaStream_t st) {
 int validate(const os_config* c) {
   if (c->width < 3 || c->height < 3)
     return set_err(OS_ERR_INVALID, "grid must be at least 3x3 (got %dx%d)", c->width, c->height);
-  if ((int64_t)c->width * c->height > (int64_t)1 << 34)
-    return set_err(OS_ERR_INVALID, "grid too large");
+  // The reference indexes cells with int (Fluid::indx, src/fluid.cu:163-165),
+  // so its grids stay below 2^31 cells; the library's gathers use 32-bit
+  // indices over the grid and its one-cell ring.
+  if ((int64_t)(c->width + 2) * (c->height + 2) > INT32_MAX)
+    return set_err(OS_ERR_INVALID, "grid too large: (width + 2) * (height + 2) must be below 2^31");
   if ((int)c->cell_size < 1)
     return set_err(OS_ERR_INVALID, "sim.cell_size must be >= 1 (Fluid truncates it to int)");
   if (c->projection_n < 0) return set_err(OS_ERR_INVALID, "sim.projection.n must be >= 0");
@@ -962,6 +965,19 @@ int os_synchronize(os_handle* h) {
   return check_resident(h);
 }
 
+int os_query(os_handle* h, int32_t* idle) {
+  if (!h || !idle) return set_err(OS_ERR_INVALID, "null argument");
+  *idle = 0;
+  int rc = select_device(h);
+  if (rc) return rc;
+  const cudaError_t e = cudaStreamQuery(h->stream);
+  if (e == cudaErrorNotReady) return OS_OK;
+  if (e != cudaSuccess) return set_err(OS_ERR_CUDA, "stream query: %s", cudaGetErrorString(e));
+  if ((rc = check_resident(h))) return rc;
+  *idle = 1;
+  return OS_OK;
+}
+
 int os_update(os_handle* h, const os_source* src, float dt) {
   int rc = os_update_async(h, src, dt, 1, nullptr);
   if (rc) return rc;
@@ -1265,6 +1281,68 @@ int os_selftest_bounded_wait(int32_t device, int32_t* status) {
   if (dev_err) cudaFree(dev_err);
   if (host_err) cudaFreeHost(host_err);
   if (e != cudaSuccess) return set_err(OS_ERR_CUDA, "self-test: %s", cudaGetErrorString(e));
+  return OS_OK;
+}
+
+namespace {
+
+// One pass of the bandwidth probe: every thread copies its float4 elements
+// of the buffer `reps` times, alternating direction (a -> b, then b -> a),
+// with cache-at-L2 loads and stores in volatile inline PTX, so that no copy
+// is elided or served from L1. Grid-stride over n4 elements.
+__global__ void k_probe_copy(float4* a, float4* b, int64_t n4, int reps) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int r = 0; r < reps; r++) {
+    float4* src = (r & 1) ? b : a;
+    float4* dst = (r & 1) ? a : b;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n4; k += stride) {
+      float4 x;
+      asm volatile("ld.global.cg.v4.f32 {%0, %1, %2, %3}, [%4];"
+                   : "=f"(x.x), "=f"(x.y), "=f"(x.z), "=f"(x.w)
+                   : "l"(src + k));
+      asm volatile("st.global.cg.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(dst + k), "f"(x.x),
+                   "f"(x.y), "f"(x.z), "f"(x.w)
+                   : "memory");
+    }
+  }
+}
+
+}  // namespace
+
+int os_probe_copy_bandwidth(int32_t device, uint64_t bytes, int32_t reps, float* gbs) {
+  if (!gbs || reps < 1 || bytes < 16 || (bytes & 15))
+    return set_err(OS_ERR_INVALID, "probe: bytes must be a positive multiple of 16, reps >= 1");
+  *gbs = 0.0f;
+  CUDA_OR_RETURN(cudaSetDevice(device));
+  float4* a = nullptr;
+  float4* b = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaStream_t st = nullptr;
+  cudaError_t e = cudaMalloc(&a, bytes);
+  if (e == cudaSuccess) e = cudaMalloc(&b, bytes);
+  if (e == cudaSuccess) e = cudaMemset(a, 0, bytes);
+  if (e == cudaSuccess) e = cudaMemset(b, 0, bytes);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  const int64_t n4 = (int64_t)(bytes / 16);
+  const int blocks = sm_count(device) * 4;
+  if (e == cudaSuccess) {
+    k_probe_copy<<<blocks, 512, 0, st>>>(a, b, n4, 2);  // first touch
+    cudaEventRecord(e0, st);
+    k_probe_copy<<<blocks, 512, 0, st>>>(a, b, n4, reps);
+    cudaEventRecord(e1, st);
+    e = cudaEventSynchronize(e1);
+  }
+  float ms = 0.0f;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+  if (e == cudaSuccess && ms > 0.0f) *gbs = (float)(2.0 * (double)bytes * reps / (ms * 1e-3) / 1e9);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (st) cudaStreamDestroy(st);
+  if (a) cudaFree(a);
+  if (b) cudaFree(b);
+  if (e != cudaSuccess) return set_err(OS_ERR_CUDA, "probe: %s", cudaGetErrorString(e));
   return OS_OK;
 }
 

@@ -249,6 +249,12 @@ class Fluid:
     def synchronize(self) -> None:
         check(self._lib.os_synchronize(self._h))
 
+    def idle(self) -> bool:
+        """True when every step enqueued on the handle's own stream has run."""
+        out = C.c_int32()
+        check(self._lib.os_query(self._h, C.byref(out)))
+        return bool(out.value)
+
     def run_phase(self, phase: int, source: Source | None, d_t: float) -> None:
         src = (source or Source()).to_native()
         check(self._lib.os_run_phase(self._h, int(phase), C.byref(src), C.c_float(d_t)))

@@ -118,6 +118,7 @@ SIGNATURES = [
     ("os_update", C.c_int, [C.c_void_p, C.POINTER(OsSource), C.c_float]),
     ("os_update_async", C.c_int, [C.c_void_p, C.POINTER(OsSource), C.c_float, C.c_int32, C.c_void_p]),
     ("os_synchronize", C.c_int, [C.c_void_p]),
+    ("os_query", C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     ("os_fields", C.c_int, [C.c_void_p, C.POINTER(OsFieldsView)]),
     ("os_upload", C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_size_t]),
     ("os_download", C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_size_t]),
@@ -136,6 +137,8 @@ SIGNATURES = [
     ("os_render_traces", C.c_int, [C.c_void_p, C.c_void_p, C.c_float, C.c_void_p, C.c_void_p,
                                    C.c_void_p]),
     ("os_selftest_bounded_wait", C.c_int, [C.c_int32, C.POINTER(C.c_int32)]),
+    ("os_probe_copy_bandwidth", C.c_int, [C.c_int32, C.c_uint64, C.c_int32,
+                                          C.POINTER(C.c_float)]),
     ("os_batch_create", C.c_int, [C.POINTER(OsConfig), C.c_int32, C.c_int32,
                                   C.POINTER(C.c_void_p)]),
     ("os_batch_create_dynamic", C.c_int, [C.c_int32, C.c_int32, C.c_uint64,

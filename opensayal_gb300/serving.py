@@ -1,13 +1,17 @@
 """Serving wind-tunnel scenarios as they arrive (continuous batching).
 
-`Server.run` takes requests with arrival times and serves them through one
-dynamic Batch: arrivals queue in order; a request is admitted when a member
-slot is free and its fields fit the device-memory budget (the batch refuses
-what does not fit without touching the device); admitted requests join the
-shared steps, each stops after exactly its own step count, and its result
-(the smoke field) is read back as soon as its last step has completed, which
-frees its memory for the next request. `serve_serial` is the baseline: the
-same requests one at a time through a single Fluid handle each.
+`Server.run` takes requests with arrival times and serves them as they
+arrive: waiting requests are taken shortest remaining work first (with an
+ageing bound); a request runs in a latency lane (a single handle on its own
+stream, concurrent with the others) when one is free, and otherwise joins
+one dynamic Batch, admitted while its fields fit the device-memory budget
+(the batch refuses what does not fit without touching the device) and the
+batch is below the size at which its throughput saturates. Every request
+stops after exactly its own step count, and its result (the smoke field) is
+read back as soon as its last step has completed, which frees its lane or
+memory for the next request. `serve_serial` is the baseline: the same
+requests one at a time, in arrival order, through a single Fluid handle
+each.
 
 Time-to-result is measured from a request's arrival to the end of its result's
 device-to-host read. A run ends at the horizon; requests not finished by then
@@ -79,22 +83,92 @@ def _initial_fields(view: Fluid, req: Request) -> int:
     return u.nbytes + v.nbytes
 
 
+class HandleLane:
+    """One request on a single handle of its own, stepping on the handle's own
+    stream: lanes run concurrently with one another and with the batch. Steps
+    are enqueued in chunks; a chunk that finished in under `target_s` doubles
+    the next one (up to 256 steps), so short steps do not leave the device
+    waiting for the host."""
+
+    def __init__(self, req: Request, block_k: int = 8, target_s: float = 0.01,
+                 clock=time.perf_counter):
+        c = req.config.copy()
+        c.projection_block = block_k
+        self.req, self.clock, self.target_s = req, clock, target_s
+        self.f = Fluid(c)
+        self.h2d_bytes = _initial_fields(self.f, req)
+        self.device_bytes = 40 * req.cells  # u, v, smoke (+buffers), p, masks, flags
+        self.done = 0         # steps known complete
+        self.in_flight = 0    # steps enqueued and not yet known complete
+        self.chunk = 16
+        self.t_enq = 0.0
+
+    def pump(self) -> None:
+        """Record a completed chunk and enqueue the next one; never waits."""
+        if self.in_flight:
+            if not self.f.idle():
+                return
+            self.done += self.in_flight
+            if self.clock() - self.t_enq < self.target_s:
+                self.chunk = min(256, self.chunk * 2)
+            self.in_flight = 0
+        left = self.req.steps - self.done
+        if left > 0:
+            k = min(self.chunk, left)
+            self.f.update_async(None, self.req.config.d_t, k)
+            self.in_flight = k
+            self.t_enq = self.clock()
+
+    @property
+    def finished(self) -> bool:
+        return self.done == self.req.steps
+
+    def result(self) -> np.ndarray:
+        return self.f.download("smoke")
+
+    def wait(self) -> None:
+        self.f.synchronize()
+        self.done += self.in_flight
+        self.in_flight = 0
+
+    def close(self) -> None:
+        self.f.close()
+
+
 class Server:
-    """Continuous batching over one dynamic Batch.
+    """Continuous batching over one dynamic Batch, with latency lanes.
 
-    max_members bounds the requests on the GPU at once (the batch's step time
-    grows with their cells); chunk is the number of steps enqueued per loop
-    turn and depth the chunks allowed in flight before the loop waits. `batch`
-    replaces the dynamic Batch the server would create (any object with its
-    add/remove/step/wait/poll/status/memory/scenario/stats/synchronize)."""
+    Waiting requests are taken shortest remaining work first (cells x steps),
+    except that a request that has waited `age_limit_s` goes ahead of all
+    younger ones in arrival order, so that no request starves. A request goes
+    to a free lane when there is one (`lanes` single handles, each on its own
+    stream, running concurrently: at light load a request runs at the speed
+    of a grid alone, without queueing behind the one before it); otherwise it
+    joins the batch, which steps all its members with one graph per step. The
+    batch admits members while their fields fit the device-memory budget and
+    the cells in it stay within `saturation_cells` (beyond which the batch's
+    throughput no longer grows and every member only slows down), and, when
+    `max_members` is set, while it has fewer members. `chunk` is the number
+    of batch steps enqueued per loop turn and `depth` the chunks allowed in
+    flight before the loop waits. `batch` replaces the dynamic Batch the
+    server would create (any object with its add/remove/step/wait/poll/status/
+    memory/scenario/stats/synchronize) and `lane_factory` the lanes (a
+    callable taking a request; the result needs pump/finished/result/wait/
+    close and h2d_bytes/device_bytes)."""
 
-    def __init__(self, budget_bytes: int, block_k: int = 8, max_members: int = 64,
-                 chunk: int = 2, depth: int = 2, device: int = 0, batch=None):
+    def __init__(self, budget_bytes: int, block_k: int = 8, max_members: int | None = None,
+                 chunk: int = 2, depth: int = 2, device: int = 0, batch=None, lanes: int = 0,
+                 saturation_cells: int | None = None, age_limit_s: float = 30.0,
+                 lane_factory=None):
         self.batch = batch if batch is not None else Batch.dynamic(
             block_k=block_k, device=device, budget_bytes=budget_bytes)
         self.max_members = max_members
         self.chunk = chunk
         self.depth = depth
+        self.lanes = lanes
+        self.saturation_cells = saturation_cells
+        self.age_limit_s = age_limit_s
+        self.lane_factory = lane_factory or (lambda req: HandleLane(req, block_k))
 
     def close(self):
         self.batch.close()
@@ -105,56 +179,99 @@ class Server:
     def __exit__(self, *exc):
         self.close()
 
+    def _pick(self, queue: list, now: float) -> int:
+        """Index of the next request to serve: the oldest of those past the age
+        limit, else the least work (cells x steps), ties in arrival order."""
+        best, best_key = 0, None
+        for k, r in enumerate(queue):
+            aged = now - r.arrival >= self.age_limit_s
+            key = (0, r.arrival) if aged else (1, r.cells * r.steps, r.arrival)
+            if best_key is None or key < best_key:
+                best, best_key = k, key
+        return best
+
     def run(self, requests: list[Request], horizon_s: float, results: dict | None = None,
             clock=time.perf_counter, sleep=time.sleep) -> ServeReport:
         b = self.batch
         rep = ServeReport()
         pending = deque(sorted(requests, key=lambda r: r.arrival))
-        queue: deque[Request] = deque()
-        active: dict[int, tuple[Request, int]] = {}  # id -> (request, steps_enqueued at admit)
+        queue: list[Request] = []
+        active: dict[int, Request] = {}  # batch member id -> request
+        lanes: list = []
+        batch_cells = 0
         t0 = clock()
+
+        def finish(req, smoke, now):
+            rep.d2h_bytes += smoke.nbytes
+            rep.latencies_s.append(now - req.arrival)
+            rep.finished += 1
+            rep.cell_steps += req.cells * req.steps
+            if results is not None:
+                results[req.index] = smoke
+
         while True:
             now = clock() - t0
             while pending and pending[0].arrival <= now:
-                queue.append(pending.popleft())
+                r = pending.popleft()
+                queue.append(r)
                 rep.arrived += 1
-                rep.offered_cell_steps += queue[-1].cells * queue[-1].steps
-            while queue and len(active) < self.max_members:
-                req = queue[0]
+                rep.offered_cell_steps += r.cells * r.steps
+            # Lanes first, then the batch, each taking the best waiting request.
+            while queue and len(lanes) < self.lanes:
+                req = queue.pop(self._pick(queue, now))
+                lane = self.lane_factory(req)
+                rep.h2d_bytes += lane.h2d_bytes
+                rep.admitted += 1
+                lanes.append(lane)
+            while queue and (self.max_members is None or len(active) < self.max_members):
+                k = self._pick(queue, now)
+                req = queue[k]
+                if (self.saturation_cells is not None and active
+                        and batch_cells + req.cells > self.saturation_cells):
+                    break
                 try:
                     mid = b.add(req.config, req.steps)
                 except BudgetFull:
                     rep.budget_refusals += 1
                     break
+                queue.pop(k)
                 rep.h2d_bytes += _initial_fields(b.scenario(mid), req)
-                queue.popleft()
-                active[mid] = (req, b.stats().steps_enqueued)
+                active[mid] = req
+                batch_cells += req.cells
                 rep.admitted += 1
-            rep.peak_members = max(rep.peak_members, len(active))
-            rep.peak_device_bytes = max(rep.peak_device_bytes, b.memory()[0])
+            rep.peak_members = max(rep.peak_members, len(active) + len(lanes))
+            rep.peak_device_bytes = max(rep.peak_device_bytes,
+                                        b.memory()[0] + sum(x.device_bytes for x in lanes))
+            for lane in lanes:
+                lane.pump()
             if active:
                 b.step(self.chunk)
                 b.wait(self.depth * self.chunk)
             for mid in b.poll():
-                req, _ = active.pop(mid)
-                smoke = b.scenario(mid).download("smoke")
-                rep.d2h_bytes += smoke.nbytes
-                rep.latencies_s.append(clock() - t0 - req.arrival)
-                rep.finished += 1
-                rep.cell_steps += req.cells * req.steps
-                if results is not None:
-                    results[req.index] = smoke
+                req = active.pop(mid)
+                batch_cells -= req.cells
+                finish(req, b.scenario(mid).download("smoke"), clock() - t0)
                 b.remove(mid)
+            for lane in [x for x in lanes if x.finished]:
+                finish(lane.req, lane.result(), clock() - t0)
+                lane.close()
+                lanes.remove(lane)
             now = clock() - t0
-            if now >= horizon_s or (not pending and not queue and not active):
+            if now >= horizon_s or (not pending and not queue and not active and not lanes):
                 break
-            if not active and not queue and pending:
+            if not active and not queue and not lanes and pending:
                 sleep(max(0.0, min(pending[0].arrival - now, horizon_s - now)))
-        # Progress of the unfinished members counts toward the served work.
+            elif not active and lanes:
+                sleep(0.0005)  # lanes only: poll their streams without spinning hard
+        # Progress of the unfinished members and lanes counts toward the served work.
         b.synchronize()
-        for mid, (req, _) in active.items():
+        for mid, req in active.items():
             state, left = b.status(mid)
             rep.cell_steps += req.cells * (req.steps - max(left, 0))
+        for lane in lanes:
+            lane.wait()
+            rep.cell_steps += lane.req.cells * lane.done
+            lane.close()
         rep.wall_s = clock() - t0
         # Requests that arrived before the end but were never taken up.
         rep.arrived += sum(1 for r in pending if r.arrival < rep.wall_s)

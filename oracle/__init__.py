@@ -180,6 +180,7 @@ def _load_harness():
                                           C.c_void_p]
         lib.ref_render_arrows.argtypes = [C.c_void_p, C.c_int, C.c_float, C.c_float, C.c_float,
                                           C.c_float, C.c_int, C.c_void_p]
+        lib.ref_sample_velocity.argtypes = [C.c_void_p, C.c_int, _f32p, _f32p, _f32p, _f32p]
         rc = lib.ref_open(str(REF_CUBIN).encode())
         if rc != 0:
             raise RuntimeError(f"reference cubin: {lib.ref_last_error().decode()}")
@@ -275,6 +276,15 @@ class RefFluid:
                                       ys.ctypes.data_as(C.c_void_p)):
             raise RuntimeError(self.lib.ref_last_error().decode())
         return xs, ys
+
+    def sample_velocity(self, px: np.ndarray, py: np.ndarray):
+        """The reference's get_general_velocity at the points (px, py)."""
+        px = np.ascontiguousarray(px, dtype=np.float32)
+        py = np.ascontiguousarray(py, dtype=np.float32)
+        ou, ov = np.empty_like(px), np.empty_like(py)
+        if self.lib.ref_sample_velocity(self.h, px.size, px, py, ou, ov):
+            raise RuntimeError(self.lib.ref_last_error().decode())
+        return ou, ov
 
     def render_arrows(self, cell_size: int, length_multiplier: float, disable_threshold: float,
                       head_length: float, head_angle: float, distance: int,

@@ -356,7 +356,7 @@ int ref_pressure_range(void* h, float* mn, float* mx) {
 // ---------------------------------------------------------------------------
 
 cudaLibrary_t g_vlib = nullptr;
-cudaKernel_t g_vpixels, g_vtraces, g_varrows;
+cudaKernel_t g_vpixels, g_vtraces, g_varrows, g_vsample;
 
 int ref_visual_open(const char* cubin_path) {
   if (g_vlib) return 0;
@@ -365,7 +365,8 @@ int ref_visual_open(const char* cubin_path) {
   if (e != cudaSuccess) return fail("cudaLibraryLoadFromFile(visual)", e);
   if ((e = cudaLibraryGetKernel(&g_vpixels, g_vlib, "ref_pixels")) != cudaSuccess ||
       (e = cudaLibraryGetKernel(&g_vtraces, g_vlib, "ref_traces")) != cudaSuccess ||
-      (e = cudaLibraryGetKernel(&g_varrows, g_vlib, "ref_arrows")) != cudaSuccess)
+      (e = cudaLibraryGetKernel(&g_varrows, g_vlib, "ref_arrows")) != cudaSuccess ||
+      (e = cudaLibraryGetKernel(&g_vsample, g_vlib, "ref_sample")) != cudaSuccess)
     return fail("visual kernels", e);
   return 0;
 }
@@ -425,6 +426,27 @@ int ref_render_arrows(void* h, int cell_size, float length_multiplier, float dis
   const int rc = run_inout((const void*)g_varrows, grid, block, args, d, inout, bytes);
   cudaFree(d);
   return rc;
+}
+
+// The reference's get_general_velocity at n points (px, py) -> (u, v).
+int ref_sample_velocity(void* h, int n, const float* px, const float* py, float* ou, float* ov) {
+  Ref* r = static_cast<Ref*>(h);
+  if (n < 1) return 0;
+  const size_t bytes = (size_t)n * sizeof(float);
+  float* d = nullptr;
+  if (cudaMalloc(&d, 4 * bytes) != cudaSuccess) return fail("cudaMalloc", cudaErrorMemoryAllocation);
+  float *dx = d, *dy = d + n, *du = d + 2 * (size_t)n, *dv = d + 3 * (size_t)n;
+  cudaError_t e = cudaMemcpy(dx, px, bytes, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dy, py, bytes, cudaMemcpyHostToDevice);
+  void* args[] = {&r->d_this, &dx, &dy, &n, &du, &dv};
+  if (e == cudaSuccess)
+    e = cudaLaunchKernel((const void*)g_vsample, dim3((n + 127) / 128), dim3(128), args, 0,
+                         (cudaStream_t)0);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(ou, du, bytes, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(ov, dv, bytes, cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  return e == cudaSuccess ? 0 : fail("sample kernel", e);
 }
 
 }  // extern "C"

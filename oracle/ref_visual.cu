@@ -14,7 +14,9 @@
 //     the reference's Fluid::trace (src/fluid.cu:16-36);
 //   * ref_arrows: update_center_velocity_arrow_kernel / _at (:304-335) and
 //     make_arrow_data (:168-200), restated, calling the reference's
-//     Fluid::get_general_velocity (src/fluid.cu:541-545).
+//     Fluid::get_general_velocity (src/fluid.cu:541-545);
+//   * ref_sample: the reference's Fluid::get_general_velocity at given
+//     points, as consumer kernels call it (src/graphics_handler.cu:269-283).
 // The Fluid object is the harness's byte-for-byte replica (ref_harness.cpp).
 // One deliberate difference: the reference's trace and arrow kernels bound
 // only the cell (i < width, j < height), so the threads of a grid that
@@ -143,4 +145,13 @@ extern "C" __global__ void ref_arrows(Fluid* d_fluid, RefArrowData* out, int cel
     a.right_head_end_y = a.end_y + arrow_y_offset;
   }
   out[(arrows_h - j / distance - 1) * arrows_w + i / distance] = a;
+}
+
+extern "C" __global__ void ref_sample(Fluid* d_fluid, const float* px, const float* py, int n,
+                                      float* out_u, float* out_v) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  Vector2d<float> vel = d_fluid->get_general_velocity(px[k], py[k]);
+  out_u[k] = vel.get_x();
+  out_v[k] = vel.get_y();
 }

@@ -3,56 +3,94 @@ the reference's own kernels (the unmodified src/fluid.cu device code through
 oracle/ref_harness.cpp), in the form the measurements run them:
 
 * the 1920x1080 default tunnel with the autotuned kernels (temporally blocked,
-  resident projection), 100 steps;
+  resident projection), 100 steps, viscous and inviscid;
 * batched uneven tunnels (seed 4, n in {50, 100, 200}, non-integer radii)
   advanced together inside one Batch, each member against its own reference
   run;
 * the 4096x4096 tunnel (n = 200) on the pass-by-pass blocked engine.
 
-Bars (relative L2 per field): 1e-5, the bar this path is held to; 1e-4 with
-the drain open, where the reference's extrapolation races on v(W-1, 1)
-(src/fluid.cu:720-733) and two runs of the reference itself differ.
+The reference is not deterministic: its diffusion sweeps u in place from
+racing threads (src/fluid.cu:167-190), and with the drain open its
+extrapolation writes v(W-1, 1) from two threads (src/fluid.cu:720-733). Each
+case therefore runs the reference twice and measures its own spread s (the
+relative L2 between its two runs). The bar for the library against the
+reference is max(1e-5, 2 s) per field: 1e-5 where the reference repeats
+itself, and twice its own disagreement where it does not.
+
+The drain race is different in kind: on some grids the reference resolves it
+the same way run after run, and on some of those the other way from the
+library (which writes 0, the outcome on most grids). Which way a grid goes is
+read from one run of the reference's extrapolation kernel on a marked state.
+Where it writes the other value, the case is held to 1e-3 and its twin with
+the drain closed (no race) to the bar above.
 """
 import numpy as np
 import pytest
 
 import oracle
-from opensayal_gb300 import Fluid, scenarios
+from opensayal_gb300 import Fluid, native, scenarios
 from opensayal_gb300.batch import Batch
-from tests.parity_cases import FIELDS, perturbed_state
+from tests.parity_cases import FIELDS, perturbed_state, random_state
 
 pytestmark = pytest.mark.gpu
 
-REL_L2_BAR = 1e-5
-DRAIN_RACE_BAR = 1e-4
+FLOOR = 1e-5
+OTHER_RACE_OUTCOME_BAR = 1e-3
 
 
-def bar(cfg) -> float:
-    return DRAIN_RACE_BAR if cfg.enable_drain else REL_L2_BAR
-
-
-def check_fields(got: dict, ref: "oracle.RefFluid", cfg, label: str) -> None:
-    for field in FIELDS:
-        b = ref.download(field)
-        a = got[field]
-        assert np.isfinite(a).all(), f"{label}/{field}: non-finite values"
-        e = oracle.rel_l2(a, b)
-        assert e <= bar(cfg), f"{label}/{field}: rel L2 {e:.3e} > {bar(cfg):g}"
-
-
-def run_ref(cfg, state: dict, steps: int) -> "oracle.RefFluid":
+def run_ref(cfg, state: dict, steps: int) -> dict:
     r = oracle.RefFluid(cfg)
     for k, a in state.items():
         r.upload(k, a)
     for _ in range(steps):
         r.update(None, cfg.d_t)
-    return r
+    out = {k: r.download(k) for k in FIELDS}
+    r.close()
+    return out
+
+
+def reference_race_zeroes(cfg) -> bool:
+    """True when the reference's extrapolation leaves v(W-1, 1) at 0 (the
+    library's resolution) on this grid, False when it copies v(W-2, 1)."""
+    if not cfg.enable_drain:
+        return True
+    W, H = cfg.width, cfg.height
+    base = oracle.OracleFluid(cfg)
+    state = random_state(cfg, 77, base.is_solid)
+    k = (H - 1 - 1) * W  # row j = 1
+    state["vel_y"][k + W - 2] = 0.75  # v(W-2, 1): a value the copy would carry
+    r = oracle.RefFluid(cfg)
+    for name, a in state.items():
+        r.upload(name, a)
+    r.phase(native.PHASE_EXTRAPOLATION, None, cfg.d_t)
+    got = float(r.download("vel_y")[k + W - 1])
+    r.close()
+    return got == 0.0
+
+
+def check_against_reference(got: dict, cfg, state: dict, steps: int, label: str) -> dict:
+    a = run_ref(cfg, state, steps)
+    b = run_ref(cfg, state, steps)
+    zeroes = reference_race_zeroes(cfg)
+    report = {}
+    for field in FIELDS:
+        x = got[field]
+        assert np.isfinite(x).all(), f"{label}/{field}: non-finite values"
+        spread = oracle.rel_l2(b[field], a[field])
+        bar = max(FLOOR, 2 * spread) if zeroes else OTHER_RACE_OUTCOME_BAR
+        e = oracle.rel_l2(x, a[field])
+        report[field] = (e, spread)
+        assert e <= bar, (f"{label}/{field}: rel L2 {e:.3e} > {bar:.1e} (reference spread "
+                          f"{spread:.1e}, race {'zero' if zeroes else 'copy'})")
+    return report
 
 
 @pytest.mark.parametrize("drain", [1, 0])
-def test_default_tunnel_as_benched_100_steps(gpu, drain):
+@pytest.mark.parametrize("viscosity", [0.001, 0.0])
+def test_default_tunnel_as_benched_100_steps(gpu, drain, viscosity):
     cfg = scenarios.default_tunnel_config()  # depths and forms autotuned
     cfg.enable_drain = drain
+    cfg.viscosity = viscosity
     state = perturbed_state(cfg, 2)
     with Fluid(cfg) as f:
         view = f.fields()
@@ -62,11 +100,9 @@ def test_default_tunnel_as_benched_100_steps(gpu, drain):
         f.update_async(None, cfg.d_t, 100)
         f.synchronize()
         got = {k: f.download(k) for k in FIELDS}
-        label = (f"1920x1080 drain={drain} block={view.projection_block} "
-                 f"resident={view.projection_resident}")
-    ref = run_ref(cfg, state, 100)
-    check_fields(got, ref, cfg, label)
-    ref.close()
+        label = (f"1920x1080 drain={drain} viscosity={viscosity} "
+                 f"block={view.projection_block} resident={view.projection_resident}")
+    check_against_reference(got, cfg, state, 100, label)
 
 
 def batched_members(drain: int | None):
@@ -100,10 +136,9 @@ def test_batched_scenarios_vs_reference_20_steps(gpu, drain):
         b.synchronize()
         got = [{k: b.scenario(m).download(k) for k in FIELDS} for m in range(len(members))]
     for m, (i, c) in enumerate(members):
-        ref = run_ref(c, states[m], 20)
-        check_fields(got[m], ref, c, f"scenario {i} ({c.width}x{c.height}, n={c.projection_n}, "
-                                     f"r={c.obstacle_radius:.3f})")
-        ref.close()
+        check_against_reference(got[m], c, states[m], 20,
+                                f"scenario {i} ({c.width}x{c.height}, n={c.projection_n}, "
+                                f"r={c.obstacle_radius:.3f}, drain={c.enable_drain})")
 
 
 @pytest.mark.parametrize("drain", [1, 0])
@@ -118,6 +153,4 @@ def test_large_grid_3_steps(gpu, drain):
             f.update(None, cfg.d_t)
         got = {k: f.download(k) for k in FIELDS}
         assert f.fields().projection_block > 0
-    ref = run_ref(cfg, state, 3)
-    check_fields(got, ref, cfg, f"4096x4096 drain={drain}")
-    ref.close()
+    check_against_reference(got, cfg, state, 3, f"4096x4096 drain={drain}")

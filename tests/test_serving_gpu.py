@@ -141,7 +141,8 @@ def test_unlimited_member_runs_until_removed(gpu):
         assert b.stats().members_in_plan == 0
 
 
-def test_served_results_equal_serial_solves(gpu):
+@pytest.mark.parametrize("lanes", [0, 2])
+def test_served_results_equal_serial_solves(gpu, lanes):
     from opensayal_gb300.scenarios import Request
     from opensayal_gb300.serving import Server, serve_serial
     rng = np.random.default_rng(11)
@@ -151,9 +152,9 @@ def test_served_results_equal_serial_solves(gpu):
         c = cfg_of(w, h, int(rng.choice([9, 16, 30])), BF16 if i % 2 else F32, i)
         reqs.append(Request(i, 0.002 * i, c, int(rng.integers(5, 40)), 1000 + i))
     got, want = {}, {}
-    with Server(budget_bytes=64 << 20, block_k=8, max_members=3, chunk=2) as s:
+    with Server(budget_bytes=64 << 20, block_k=8, max_members=3, chunk=2, lanes=lanes) as s:
         rep = s.run(reqs, horizon_s=300.0, results=got)
-    assert rep.finished == rep.arrived == len(reqs) and rep.peak_members <= 3
+    assert rep.finished == rep.arrived == len(reqs) and rep.peak_members <= 3 + lanes
     assert rep.cell_steps == sum(r.cells * r.steps for r in reqs)
     serial = serve_serial(reqs, horizon_s=300.0, block_k=8, results=want)
     assert serial.finished == len(reqs)

@@ -1,9 +1,10 @@
-"""The serving loop's host logic on the CPU, against a stand-in for the
-dynamic batch with a simulated clock: arrivals queue in order, admission
-respects the member limit and the memory budget (a refused request waits at
-the head of the queue), a member's result is read back when its last step has
-run, the horizon cuts the run, and the report counts unfinished requests and
-the partial progress of unfinished members."""
+"""The serving loop's host logic on the CPU, against stand-ins for the
+dynamic batch and the latency lanes with a simulated clock: waiting requests
+are taken shortest work first with an ageing bound, lanes take requests
+before the batch, admission respects the member limit, the saturation size
+and the memory budget (a refused request waits), a member's result is read
+back when its last step has run, the horizon cuts the run, and the report
+counts unfinished requests and the partial progress of unfinished members."""
 import numpy as np
 import pytest
 
@@ -55,6 +56,7 @@ class FakeBatch:
         self.used = 0
         self.next_id = 0
         self.admitted = []
+        self.admitted_steps = []
 
     def add(self, cfg, steps):
         need = 10 * cfg.width * cfg.height
@@ -66,6 +68,7 @@ class FakeBatch:
         self.views[mid] = View(cfg)
         self.used += need
         self.admitted.append(mid)
+        self.admitted_steps.append(steps)
         return mid
 
     def remove(self, mid):
@@ -170,3 +173,76 @@ def test_percentiles_over_all_arrivals():
     assert p["p50_finished_s"] == pytest.approx(2.0)
     assert p["p50_all_s"] == pytest.approx(2.0)  # rank 2 of 4 is finished
     assert p["p99_all_s"] is None                # rank 4 of 4 is not
+
+
+class FakeLane:
+    """A lane that completes one step per pump."""
+
+    def __init__(self, req, log):
+        self.req, self.done = req, 0
+        self.h2d_bytes, self.device_bytes = 8 * req.cells, 40 * req.cells
+        log.append(req.index)
+
+    def pump(self):
+        self.done = min(self.req.steps, self.done + 1)
+
+    @property
+    def finished(self):
+        return self.done == self.req.steps
+
+    def result(self):
+        return np.full(self.req.cells, -1.0 - self.req.index, np.float32)
+
+    def wait(self):
+        pass
+
+    def close(self):
+        pass
+
+
+def test_shortest_work_first_then_ageing():
+    # Three requests wait at t = 0 for a batch of one member. Without ageing
+    # they run shortest first; with a 0.05 s ageing bound the two left when
+    # the first finishes (t = 0.1 s) have both aged and go in arrival order.
+    for age, want in ((100.0, [10, 30, 50]), (0.05, [10, 50, 30])):
+        clock = Clock()
+        fb = FakeBatch(clock)
+        srv = Server(0, max_members=1, chunk=2, batch=fb, age_limit_s=age)
+        rep = srv.run(requests([0.0, 0.0, 0.0], [50, 10, 30]), horizon_s=100.0, clock=clock,
+                      sleep=clock.sleep)
+        assert rep.finished == 3
+        assert fb.admitted_steps == want
+        assert rep.latencies_s[0] == pytest.approx(0.10)
+
+
+def test_lanes_take_requests_before_the_batch():
+    clock = Clock()
+    fb = FakeBatch(clock)
+    log = []
+    srv = Server(0, chunk=2, batch=fb, lanes=2, lane_factory=lambda r: FakeLane(r, log))
+    reqs = requests([0.0] * 5, [8, 4, 6, 2, 10])
+    results = {}
+    rep = srv.run(reqs, horizon_s=100.0, results=results, clock=clock, sleep=clock.sleep)
+    assert rep.finished == rep.admitted == 5
+    assert log[:2] == [3, 1]          # the two shortest go to the lanes
+    assert len(fb.admitted) == 3      # the rest join the batch at once
+    for k in log:
+        assert np.all(results[k] == -1.0 - k)
+    assert rep.peak_members == 5
+    assert rep.cell_steps == sum(r.cells * r.steps for r in reqs)
+
+
+def test_saturation_bounds_the_batch_and_the_slot_count_does_not():
+    clock = Clock()
+    fb = FakeBatch(clock)
+    cells = 32 * 16
+    srv = Server(0, chunk=2, batch=fb, saturation_cells=3 * cells)
+    reqs = requests([0.0] * 8, [6] * 8)
+    rep = srv.run(reqs, horizon_s=100.0, clock=clock, sleep=clock.sleep)
+    assert rep.finished == 8 and rep.peak_members == 3
+    clock = Clock()
+    fb = FakeBatch(clock)
+    srv = Server(0, chunk=2, batch=fb)  # neither slots nor saturation: all join
+    rep = srv.run(requests([0.0] * 8, [6] * 8), horizon_s=100.0, clock=clock,
+                  sleep=clock.sleep)
+    assert rep.peak_members == 8
