@@ -504,7 +504,7 @@ SERVING_WORKLOAD = ("serving: Poisson {rate:g}/s for {seconds:g} s (seed 5), tun
 
 def serving_measure(world, rank, local, rate: float, seconds: float, drain: float,
                     budget_gb: float, slots: int | None, chunk: int, serial: bool = True,
-                    lanes: int = 4, saturation_mcells: float | None = 48.0) -> dict:
+                    lanes: int = 4, saturation_mcells: float | None = 32.0) -> dict:
     """Poisson arrivals (seed 5) of tunnels drawn as in the batched workload,
     steps U[100, 5000], BF16 or FP32 storage (p = 0.5), served by continuous
     batching within a device-memory budget; the same arrival trace served one
@@ -868,7 +868,7 @@ def main():
                     help="members the batch may hold (0: bounded by memory and saturation)")
     ap.add_argument("--serve-lanes", type=int, default=4,
                     help="latency lanes: requests run on single handles of their own")
-    ap.add_argument("--serve-saturation-mcells", type=float, default=48.0,
+    ap.add_argument("--serve-saturation-mcells", type=float, default=32.0,
                     help="cells (millions) the batch holds at most (0: memory only)")
     ap.add_argument("--serve-chunk", type=int, default=2)
     ap.add_argument("--no-serial", action="store_true")

@@ -1,10 +1,16 @@
 """Storage precision against an FP64 run of the same scheme.
 
 The FP64 run (storage OS_STORAGE_F64) uses the same kernels in double with
-IEEE division. Errors grow with steps because the wake behind the obstacle
-amplifies small differences: FP32 (the reference's precision) reaches ~1-2e-3
-relative L2 after 1000 steps of the 256x128 case, FP16 storage ~0.06-0.1 and
-BF16 storage ~0.3-0.8. These tests pin the ordering and bounds at 100 steps.
+IEEE division. Measured on GB300 (relative L2 of u, v, smoke against FP64,
+256x128 case, 1000 steps): FP32 (the reference's precision) 1.0e-3,
+2.3e-3, 1.3e-3; FP16 storage 4.5e-2, 7.8e-2, 8.6e-2; BF16 storage 0.37,
+0.96, 0.66. The 1e-3 target of the reduced storage after 1000 steps is not
+met, and cannot be with this scheme: a diffusion sweep changes u by
+a * lap(u) with a = viscosity * dt = 5e-5, far below half a unit in the last
+place of a 16-bit value near the inflow speed, so 16-bit storage rounds the
+diffusion away pass after pass, and the projection's late corrections with
+it. These tests pin the ordering and the measured bounds (with margin) at 100
+and 1000 steps.
 """
 import numpy as np
 import pytest
@@ -79,3 +85,19 @@ def test_downloads_convert_storage_to_fp32(gpu):
             f.upload("vel_x", x)
             y = f.download("vel_x")
             assert np.all(np.abs(y - x) <= tol * np.abs(x) + 1e-7)
+
+
+def test_thousand_steps_against_fp64(gpu):
+    """The 1000-step check of the small tunnel, with the bounds measured on
+    GB300 (each bar about twice the measured error)."""
+    cfg = scenarios.small_config()
+    state = perturbed_state(cfg, 1)
+    steps = 1000
+    ref = run(cfg, native.STORAGE_F64, steps, state)
+    e32 = errors(run(cfg, native.STORAGE_F32, steps, state), ref)
+    e16 = errors(run(cfg, native.STORAGE_F16, steps, state), ref)
+    eb16 = errors(run(cfg, native.STORAGE_BF16, steps, state), ref)
+    assert max(e32.values()) < 5e-3, e32
+    assert max(e16.values()) < 0.2, e16
+    assert max(eb16.values()) < 2.0, eb16
+    assert max(e32.values()) < max(e16.values()) < max(eb16.values()), (e32, e16, eb16)
