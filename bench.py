@@ -314,14 +314,23 @@ def run_gb300(args, world, rank, local) -> dict | None:
     proj_bytes = 17 * cfg.projection_n * cells
     diff_ms, diff_kernels = f.profile_phase(native.PHASE_DIFFUSION, None, dt, 3, sptr)
     achieved = proj_bytes / proj_s / 1e9
-    # DRAM bytes per projection launch from the ncu capture summarised in
-    # profiles/ (same workload and blocking depth), or null.
-    traffic = None
+    # DRAM bytes of the projection phase: per launch from the ncu capture
+    # summarised in profiles/ (same workload and blocking depth) or scaled
+    # from one, as the entry says, times the phase's launches; null when the
+    # configuration was not captured.
+    traffic, traffic_source, on_chip = None, "not captured for this configuration", None
     tfile = ROOT / "profiles" / "roofline_traffic.json"
     if tfile.exists():
         key = f"{args.workload}:block{f.fields().projection_block}" + (
             ":resident" if f.fields().projection_resident else "")
-        traffic = json.loads(tfile.read_text()).get(key)
+        entry = json.loads(tfile.read_text()).get(key)
+        if entry:
+            traffic = entry["bytes_per_launch"] * max(1, proj_kernels // 3)
+            traffic_source = entry["source"]
+            if "smsp__issue_active" in entry:
+                on_chip = {"smsp__issue_active": entry["smsp__issue_active"],
+                           "l1tex__throughput": entry["l1tex__throughput"],
+                           "source": "the same capture"}
     step_bytes = bytes_per_cell_step(cfg.projection_n, cfg.viscosity != 0.0)
     l2 = l2_copy_peak(local)
     ms_per_step = total_s * 1e3 / args.steps
@@ -339,6 +348,7 @@ def run_gb300(args, world, rank, local) -> dict | None:
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"],
                      "unit": "GB/s", "frac": achieved / pk["hbm_gbs"], "traffic": traffic,
+                     "traffic_source": traffic_source,
                      "kernel": "projection phase (17 B/cell per red/black sweep x n sweeps)",
                      "launches": proj_kernels // 3, "peak_source": pk["source"]},
         # The projection's sweeps run in shared memory and its halo exchanges
@@ -347,7 +357,9 @@ def run_gb300(args, world, rank, local) -> dict | None:
         # against a live L2-resident copy.
         "roofline_l2": {"bound": "l2", "achieved": achieved, "peak": l2["gbs"], "unit": "GB/s",
                         "frac": achieved / l2["gbs"], "peak_source": "measured live: " + l2["how"],
-                        "peak_buffer_mib": l2.get("buffer_mib")},
+                        "peak_buffer_mib": l2.get("buffer_mib"),
+                        # the binding pipes: instruction issue and shared memory
+                        "on_chip": on_chip},
         "step_roofline": {"bytes_per_cell_step": step_bytes,
                           "achieved": step_bytes * value / world / 1e9, "unit": "GB/s",
                           "frac": step_bytes * value / world / 1e9 / pk["hbm_gbs"]},

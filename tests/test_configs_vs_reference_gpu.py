@@ -17,25 +17,28 @@ relative L2 between its two runs). The bar for the library against the
 reference is max(1e-5, 2 s) per field: 1e-5 where the reference repeats
 itself, and twice its own disagreement where it does not.
 
-The drain race is different in kind: on some grids the reference resolves it
-the same way run after run, and on some of those the other way from the
-library (which writes 0, the outcome on most grids). Which way a grid goes is
-read from one run of the reference's extrapolation kernel on a marked state.
-Where it writes the other value, the case is held to 1e-3 and its twin with
-the drain closed (no race) to the bar above.
+The drain race is different in kind. The library writes 0 there (the
+outcome the reference gives most often), while the reference's outcome can
+change from step to step and from one GPU to another: the 1920x1080 tunnel
+without diffusion has ended 3.7e-6 from the library on one GB300 and 1.1e-4
+on another, and a 448x704 member 1.1e-4, each time with the reference's two
+runs agreeing to a few 1e-6. With the drain open a case is therefore held to
+max(1e-5, 2 s, 5e-4), about five times the largest effect of the race seen,
+and every such case has a twin with the drain closed (no race) held to
+max(1e-5, 2 s).
 """
 import numpy as np
 import pytest
 
 import oracle
-from opensayal_gb300 import Fluid, native, scenarios
+from opensayal_gb300 import Fluid, scenarios
 from opensayal_gb300.batch import Batch
-from tests.parity_cases import FIELDS, perturbed_state, random_state
+from tests.parity_cases import FIELDS, perturbed_state
 
 pytestmark = pytest.mark.gpu
 
 FLOOR = 1e-5
-OTHER_RACE_OUTCOME_BAR = 1e-3
+DRAIN_RACE_BAR = 5e-4
 
 
 def run_ref(cfg, state: dict, steps: int) -> dict:
@@ -49,39 +52,19 @@ def run_ref(cfg, state: dict, steps: int) -> dict:
     return out
 
 
-def reference_race_zeroes(cfg) -> bool:
-    """True when the reference's extrapolation leaves v(W-1, 1) at 0 (the
-    library's resolution) on this grid, False when it copies v(W-2, 1)."""
-    if not cfg.enable_drain:
-        return True
-    W, H = cfg.width, cfg.height
-    base = oracle.OracleFluid(cfg)
-    state = random_state(cfg, 77, base.is_solid)
-    k = (H - 1 - 1) * W  # row j = 1
-    state["vel_y"][k + W - 2] = 0.75  # v(W-2, 1): a value the copy would carry
-    r = oracle.RefFluid(cfg)
-    for name, a in state.items():
-        r.upload(name, a)
-    r.phase(native.PHASE_EXTRAPOLATION, None, cfg.d_t)
-    got = float(r.download("vel_y")[k + W - 1])
-    r.close()
-    return got == 0.0
-
-
 def check_against_reference(got: dict, cfg, state: dict, steps: int, label: str) -> dict:
     a = run_ref(cfg, state, steps)
     b = run_ref(cfg, state, steps)
-    zeroes = reference_race_zeroes(cfg)
     report = {}
     for field in FIELDS:
         x = got[field]
         assert np.isfinite(x).all(), f"{label}/{field}: non-finite values"
         spread = oracle.rel_l2(b[field], a[field])
-        bar = max(FLOOR, 2 * spread) if zeroes else OTHER_RACE_OUTCOME_BAR
+        bar = max(FLOOR, 2 * spread, DRAIN_RACE_BAR if cfg.enable_drain else 0.0)
         e = oracle.rel_l2(x, a[field])
         report[field] = (e, spread)
         assert e <= bar, (f"{label}/{field}: rel L2 {e:.3e} > {bar:.1e} (reference spread "
-                          f"{spread:.1e}, race {'zero' if zeroes else 'copy'})")
+                          f"{spread:.1e})")
     return report
 
 
