@@ -4,9 +4,9 @@ with the CPU oracle, on identical seeded inputs.
 
 Bars (relative L2 unless stated):
 * masks, neighbour counts, inflow/drain sets: bit-exact;
-* every deterministic phase against the reference kernels: bit-exact (the
-  library performs the same FP32/FP64 operations in the same order), except
-  smoke advection, which differs by at most 4 ulp in under 1% of cells;
+* every deterministic phase against the reference kernels, smoke advection
+  included: bit-exact (the library performs the same FP32/FP64 operations in
+  the same order, with the same multiply-adds fused);
 * diffusion against the reference kernels: the reference sweeps in place from
   racing threads, the library runs Jacobi; they differ by <= 64 a^2 per sweep
   (a = viscosity*dt/h^2);
@@ -107,10 +107,6 @@ def test_phase_vs_reference_kernels(gpu, name, phase, src, drain):
         a, b = lib.download(field), ref.download(field)
         for k in racy.get(field, []):
             a[k] = b[k]  # either outcome of the race is the reference's
-        if phase == native.PHASE_SMOKE_ADVECTION and field == "smoke":
-            d = ulp_diff(a, b)
-            assert d.max() <= 4 and (d > 0).mean() < 0.01, (d.max(), (d > 0).mean())
-            continue
         assert same_bits(a, b), (
             f"{name}/{field}: {int((a != b).sum())} cells differ, max |d| = "
             f"{float(np.nanmax(np.abs(a.astype(np.float64) - b)))}")
