@@ -196,6 +196,111 @@ __device__ __forceinline__ bool wait_neighbours(const ResidentSync& S, int tx, i
   return give_up == 0;
 }
 
+// Part `part` of the halo ring: 0 the region rows [0, halo) (owned by the
+// tiles one row down, ty - 1), 1 the rows [halo + TY, RH) (the tiles one row
+// up), 2 the left quads [0, hq) of the owned rows (the tile on the left),
+// 3 the right quads (the tile on the right). Cell `it` of the part.
+__device__ __forceinline__ int ring_part_items(int part, int halo, int TY, int hq) {
+  return part < 2 ? halo * kQuads : TY * hq;
+}
+__device__ __forceinline__ void ring_part_cell(int part, int it, int halo, int TY, int hq, int* y,
+                                               int* q) {
+  if (part < 2) {
+    *y = (part ? halo + TY : 0) + it / kQuads;
+    *q = it % kQuads;
+  } else {
+    *y = halo + it / hq;
+    *q = (part == 3 ? kQuads - hq : 0) + it % hq;
+  }
+}
+
+// The halo exchange's wait and reload, part by part: each part of the ring
+// is reloaded as soon as the tiles that own it have published, instead of
+// the whole ring after all eight neighbours have. The warps are split among
+// the four parts about in proportion to their sizes (3/8 to each band, 1/8
+// to each side); each part's first warp polls its neighbours' flags (three
+// for a band, one for a side, with the same bounded wait as
+// wait_neighbours) and the part's warps meet at a named barrier of their
+// own before they load, so the acquire loads order their reloads. Ends with
+// a barrier of the whole CTA; returns false, in every thread, when a wait
+// gave up here or in another CTA (the reloaded ring is then not used).
+template <bool PRESSURE, class S>
+__device__ __forceinline__ bool exchange_ring(const ResidentSync& sync, float* smem, int RH,
+                                              const S* __restrict__ u, const S* __restrict__ v,
+                                              int W, int H, int gx0, int gy0, int halo, int TY,
+                                              bool vec, int tx, int ty, int tiles_x, int tiles_y,
+                                              unsigned want) {
+  __shared__ int give_up;
+  if (threadIdx.x == 0) give_up = 0;
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const int n_band = nw * 3 / 8, n_side = nw / 8;  // 12 and 4 of 32 warps
+  int part, w0, wn;
+  if (warp < n_band) {
+    part = 0, w0 = 0, wn = n_band;
+  } else if (warp < 2 * n_band) {
+    part = 1, w0 = n_band, wn = n_band;
+  } else if (warp < 2 * n_band + n_side) {
+    part = 2, w0 = 2 * n_band, wn = n_side;
+  } else {
+    part = 3, w0 = 2 * n_band + n_side, wn = nw - w0;
+  }
+  if (warp == w0 && lane < (part < 2 ? 3 : 1)) {
+    const int nx = part < 2 ? tx + lane - 1 : tx + (part == 2 ? -1 : 1);
+    const int ny = part < 2 ? ty + (part == 0 ? -1 : 1) : ty;
+    if (nx >= 0 && nx < tiles_x && ny >= 0 && ny < tiles_y) {
+      const unsigned* f = sync.flags + ny * tiles_x + nx;
+      for (int it = 0; (int)(ld_acquire_gpu(f) - want) < 0; it++) {
+        if (it >= kSpinLimit || (it % 64 == 63 && *(volatile int*)sync.dev_err)) {
+          if (atomicCAS(sync.dev_err, 0, 1) == 0) {
+            *(volatile int*)sync.host_err = 1;
+            __threadfence_system();
+          }
+          *(volatile int*)&give_up = 1;
+          break;
+        }
+        __nanosleep(32);
+      }
+    }
+  }
+  __syncwarp();
+  asm volatile("bar.sync %0, %1;" ::"r"(1 + part), "r"(wn * 32) : "memory");
+  if (!*(volatile int*)&give_up) {
+    const ProjPlanes P = proj_planes<PRESSURE>(smem, RH);
+    const int hq = halo / 4;
+    const int items = ring_part_items(part, halo, TY, hq);
+    const int t0 = threadIdx.x - w0 * 32, stride = wn * 32;
+    for (int base = t0; base < items; base += stride * kInFlight) {
+      float4 uq[kInFlight], vq[kInFlight];
+#pragma unroll
+      for (int r = 0; r < kInFlight; r++) {
+        const int it = base + r * stride;
+        uq[r] = vq[r] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (it < items) {
+          int y, q;
+          ring_part_cell(part, it, halo, TY, hq, &y, &q);
+          uq[r] = load_quad_cg(u, W, H, gx0 + 4 * q, gy0 + y, vec);
+          vq[r] = load_quad_cg(v, W, H, gx0 + 4 * q, gy0 + y, vec);
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < kInFlight; r++) {
+        const int it = base + r * stride;
+        if (it >= items) break;
+        int y, q;
+        ring_part_cell(part, it, halo, TY, hq, &y, &q);
+        const int s = y * kHalfW + 2 * q;
+        *reinterpret_cast<float2*>(P.ue + s) = make_float2(uq[r].x, uq[r].z);
+        *reinterpret_cast<float2*>(P.uo + s) = make_float2(uq[r].y, uq[r].w);
+        *reinterpret_cast<float2*>(P.ve + s) = make_float2(vq[r].x, vq[r].z);
+        *reinterpret_cast<float2*>(P.vo + s) = make_float2(vq[r].y, vq[r].w);
+      }
+    }
+  }
+  __syncthreads();
+  return *(volatile int*)&give_up == 0;
+}
+
 template <bool PRESSURE, class S>
 __global__ void __launch_bounds__(kBlockThreads, 1)
 k_project_resident(S* U0, S* U1, S* V0, S* V1, int cu, int cv, float* __restrict__ p,
@@ -230,12 +335,13 @@ k_project_resident(S* U0, S* U1, S* V0, S* V1, int cu, int cv, float* __restrict
     publish_rect<PRESSURE, S>(smem, RH, uo, vo, W, H, gx0, gy0, 2 * halo, TY, oq0, oq0 + hq, vec);
     publish_rect<PRESSURE, S>(smem, RH, uo, vo, W, H, gx0, gy0, 2 * halo, TY, oq1 - hq, oq1, vec);
     publish_flag(sync.flags + blockIdx.x, epoch + q + 1);
-    if (!wait_neighbours(sync, tx, ty, tiles_x, tiles_y, epoch + q + 1)) return;
-    // The halo ring from the neighbours' bands; owned cells rounded as the
-    // pass engine's write-back would round them.
+    // Owned cells rounded as the pass engine's write-back would round them
+    // (the owned cells and the ring are disjoint, so this may precede the
+    // reload), then the halo ring from the neighbours' bands, part by part.
     round_owned<PRESSURE, S>(smem, RH, halo, TX, TY);
-    reload_ring<PRESSURE, S>(smem, RH, uo, vo, W, H, gx0, gy0, halo, TY, vec);
-    __syncthreads();
+    if (!exchange_ring<PRESSURE, S>(sync, smem, RH, uo, vo, W, H, gx0, gy0, halo, TY, vec, tx,
+                                    ty, tiles_x, tiles_y, epoch + q + 1))
+      return;
   }
 }
 
