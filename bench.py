@@ -325,7 +325,12 @@ def run_gb300(args, world, rank, local) -> dict | None:
             ":resident" if f.fields().projection_resident else "")
         entry = json.loads(tfile.read_text()).get(key)
         if entry:
-            traffic = entry["bytes_per_launch"] * max(1, proj_kernels // 3)
+            # launches of the projection kernel in one phase: one resident
+            # launch, or one blocked launch per pass (the phase timed alone
+            # also copies the result back, which the step does not)
+            k_proj = (1 if f.fields().projection_resident else
+                      -(-cfg.projection_n // max(1, f.fields().projection_block)))
+            traffic = entry["bytes_per_launch"] * k_proj
             traffic_source = entry["source"]
             if "smsp__issue_active" in entry:
                 on_chip = {"smsp__issue_active": entry["smsp__issue_active"],
@@ -350,7 +355,7 @@ def run_gb300(args, world, rank, local) -> dict | None:
                      "unit": "GB/s", "frac": achieved / pk["hbm_gbs"], "traffic": traffic,
                      "traffic_source": traffic_source,
                      "kernel": "projection phase (17 B/cell per red/black sweep x n sweeps)",
-                     "launches": proj_kernels // 3, "peak_source": pk["source"]},
+                     "kernels_per_phase_timed": proj_kernels // 3, "peak_source": pk["source"]},
         # The projection's sweeps run in shared memory and its halo exchanges
         # go through L2; DRAM sees the fields about once per phase. The level
         # that binds is on-chip, so the same algorithmic rate is also given
@@ -616,6 +621,8 @@ def run_precision(args, world, rank, local) -> dict | None:
             base.obstacle_radius = base.obstacle_radius * sc
             base.smoke_height = base.height // 4
     base.device = local
+    if args.precision_inviscid:
+        base.viscosity = 0.0  # no diffusion: separates its rounding from the rest
     checkpoints = sorted({int(x) for x in str(args.precision_steps).split(",") if x})
     fields = ("vel_x", "vel_y", "smoke")
     runs = {}
@@ -894,6 +901,9 @@ def main():
                     help="precision: square grid size instead of 4096 (256: the small tunnel)")
     ap.add_argument("--precision-steps", default="100,250,500,1000",
                     help="precision: cumulative step counts at which the errors are taken")
+    ap.add_argument("--precision-inviscid", action="store_true",
+                    help="precision: viscosity 0 (the diffusion's increments are what 16-bit "
+                         "storage rounds away)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
