@@ -187,3 +187,27 @@ def test_visual_defaults_follow_config_parser(lib_built):
     assert (v.trace_distance, v.trace_length) == (20, 20)
     assert abs(v.arrow_length_multiplier - 0.1) < 1e-7 and v.arrow_disable_threshold == 0.0
     assert C.sizeof(native.OsArrow) == 36 and C.sizeof(native.OsVisualConfig) == 32
+
+
+def test_query_and_probe_reject_bad_arguments(lib_built):
+    """Argument checks come before any device work, so they hold without a GPU."""
+    lib = native.load()
+    idle = C.c_int32(7)
+    assert lib.os_query(None, C.byref(idle)) == native.OS_ERR_INVALID
+    g = C.c_float(1.0)
+    assert lib.os_probe_copy_bandwidth(0, 24, 10, C.byref(g)) == native.OS_ERR_INVALID  # not x16
+    assert lib.os_probe_copy_bandwidth(0, 1 << 20, 0, C.byref(g)) == native.OS_ERR_INVALID
+    assert lib.os_probe_copy_bandwidth(0, 1 << 20, 10, None) == native.OS_ERR_INVALID
+    text = b'{"sim": {"width": 64, "height": 32}}'
+    cfg = native.OsConfig()
+    assert lib.os_config_parse(None, 0, C.byref(cfg), None) == native.OS_ERR_INVALID
+    assert lib.os_config_parse(text, len(text), None, None) == native.OS_ERR_INVALID
+
+
+def test_grids_beyond_int_indices_are_rejected(lib_built):
+    """The reference's cell indices are int: (W + 2)(H + 2) must stay below 2^31."""
+    lib = native.load()
+    cfg = default_config(46340, 46340)  # (W + 2)(H + 2) > 2^31 - 1
+    h = C.c_void_p()
+    assert lib.os_create(C.byref(cfg), C.byref(h)) == native.OS_ERR_INVALID
+    assert b"2^31" in lib.os_last_error()
