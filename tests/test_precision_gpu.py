@@ -5,12 +5,11 @@ IEEE division. Measured on GB300 (relative L2 of u, v, smoke against FP64,
 256x128 case, 1000 steps): FP32 (the reference's precision) 1.0e-3,
 2.3e-3, 1.3e-3; FP16 storage 4.5e-2, 7.8e-2, 8.6e-2; BF16 storage 0.37,
 0.96, 0.66. The 1e-3 target of the reduced storage after 1000 steps is not
-met, and cannot be with this scheme: a diffusion sweep changes u by
-a * lap(u) with a = viscosity * dt = 5e-5, far below half a unit in the last
-place of a 16-bit value near the inflow speed, so 16-bit storage rounds the
-diffusion away pass after pass, and the projection's late corrections with
-it. These tests pin the ordering and the measured bounds (with margin) at 100
-and 1000 steps.
+met: the velocity is rounded to 16 bits every time a blocked pass writes it
+back (about 2^-12 relative in FP16, 2^-9 in BF16), and those roundings
+accumulate and are amplified by the flow; the errors are the same with the
+diffusion off. These tests pin the ordering and the measured bounds (with
+margin) at 100 and 1000 steps.
 """
 import numpy as np
 import pytest
