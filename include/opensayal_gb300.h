@@ -224,6 +224,19 @@ int os_fields(os_handle* h, os_fields_view* out);
  * Float fields are converted from / to the storage precision. */
 int os_upload(os_handle* h, int32_t field, const void* host, size_t count);
 int os_download(os_handle* h, int32_t field, void* host, size_t count);
+/*
+ * Without waiting: enqueues on `stream` (NULL: the handle's stream), after
+ * the work already there, a copy of a field as it is at that point into a
+ * caller-owned device buffer of `count` = width * height 4-byte values
+ * (storage fields converted to FP32). With the step on the same stream, a
+ * caller reads the copy to the host on a stream of its own while the next
+ * step runs: the snapshot is not touched by later steps, while the live
+ * field is (the next step's inflow writes smoke at once). No reference
+ * counterpart (the reference's callers read the fields after a synchronous
+ * update).
+ */
+int os_snapshot_async(os_handle* h, int32_t field, void* device_dst, size_t count,
+                      void* stream);
 
 /* Pressure extrema of the last step with enable_pressure set.
  * Replaces: Fluid::min_pressure / Fluid::max_pressure (src/fluid.cu:778-787). */

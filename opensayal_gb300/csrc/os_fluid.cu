@@ -1064,6 +1064,36 @@ int os_download(os_handle* h, int32_t field, void* host, size_t count) {
   return OS_OK;
 }
 
+int os_snapshot_async(os_handle* h, int32_t field, void* device_dst, size_t count,
+                      void* stream) {
+  if (!h || !device_dst) return set_err(OS_ERR_INVALID, "null argument");
+  if (count != h->N) return set_err(OS_ERR_INVALID, "count %zu != width*height %zu", count, h->N);
+  void* src;
+  bool storage_field;
+  int rc = field_target(h, field, &src, &storage_field);
+  if (rc) return rc;
+  if ((rc = select_device(h))) return rc;
+  cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : h->stream;
+  if (!storage_field || h->storage == OS_STORAGE_F32) {
+    CUDA_OR_RETURN(cudaMemcpyAsync(device_dst, src, h->N * 4, cudaMemcpyDeviceToDevice, st));
+    return OS_OK;
+  }
+  const int64_t N = (int64_t)h->N;
+  const unsigned g = (unsigned)((N + 255) / 256);
+  float* dst = static_cast<float*>(device_dst);
+  switch (h->storage) {
+    case OS_STORAGE_F16: k_to_f32<__half><<<g, 256, 0, st>>>((const __half*)src, dst, N); break;
+    case OS_STORAGE_BF16:
+      k_to_f32<__nv_bfloat16><<<g, 256, 0, st>>>((const __nv_bfloat16*)src, dst, N);
+      break;
+    case OS_STORAGE_F64: k_to_f32<double><<<g, 256, 0, st>>>((const double*)src, dst, N); break;
+    default: return set_err(OS_ERR_INVALID, "bad storage");
+  }
+  h->launches++;
+  CUDA_OR_RETURN(cudaGetLastError());
+  return OS_OK;
+}
+
 int os_diagnose(os_handle* h, os_diag* out) {
   if (!h || !out) return set_err(OS_ERR_INVALID, "null argument");
   static_assert(kDiagBytes == (kDiagBlocks + 1) * kDiagSlots * sizeof(double),

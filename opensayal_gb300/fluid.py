@@ -103,6 +103,7 @@ CONFIG_KEYS: dict[str, tuple[str, type]] = {
     "fluid.viscosity": ("viscosity", float),
 }
 
+
 class _WrongType(TypeError):
     pass
 
@@ -288,6 +289,14 @@ class Fluid:
         assert out.dtype == dtype and out.size == n and out.flags.c_contiguous
         check(self._lib.os_download(self._h, fid, out.ctypes.data_as(C.c_void_p), n))
         return out
+
+    def snapshot_async(self, field: str | int, d_dst: int, stream: int | None = None) -> None:
+        """Enqueue a copy of `field` (as FP32 or int32, width * height values)
+        into the device buffer at `d_dst` on `stream`, without waiting."""
+        fid = FIELD_IDS[field] if isinstance(field, str) else field
+        check(self._lib.os_snapshot_async(self._h, fid, C.c_void_p(d_dst),
+                                          self.width * self.height,
+                                          C.c_void_p(stream) if stream else None))
 
     def upload(self, field: str | int, data: np.ndarray) -> None:
         fid = FIELD_IDS[field] if isinstance(field, str) else field

@@ -122,6 +122,8 @@ SIGNATURES = [
     ("os_fields", C.c_int, [C.c_void_p, C.POINTER(OsFieldsView)]),
     ("os_upload", C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_size_t]),
     ("os_download", C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_size_t]),
+    ("os_snapshot_async", C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_size_t,
+                                    C.c_void_p]),
     ("os_pressure_range", C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     ("os_run_phase", C.c_int, [C.c_void_p, C.c_int32, C.POINTER(OsSource), C.c_float]),
     ("os_kernel_launches", C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
