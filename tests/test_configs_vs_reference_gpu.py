@@ -143,3 +143,35 @@ def test_large_grid_3_steps(gpu, drain):
         got = {k: f.download(k) for k in FIELDS}
         assert f.fields().projection_block > 0
     check_against_reference(got, cfg, state, 3, f"4096x4096 drain={drain}")
+
+
+def test_default_tunnel_with_pressure_20_steps(gpu):
+    """sim.enable_pressure on the benchmarked grid: the resident projection
+    accumulates p in its sweeps and the extrema come from the warp-shuffle
+    reduction. Without diffusion and with the drain closed nothing races, so
+    every field, pressure included, must equal the reference's bit for bit,
+    and so must the extrema (the reference's Thrust reductions)."""
+    cfg = scenarios.default_tunnel_config()
+    cfg.enable_pressure = 1
+    cfg.enable_drain = 0
+    cfg.viscosity = 0.0
+    state = perturbed_state(cfg, 6)
+    with Fluid(cfg) as f:
+        assert f.fields().projection_block > 0
+        for k, a in state.items():
+            f.upload(k, a)
+        for _ in range(20):
+            f.update(None, cfg.d_t)
+        got = {k: f.download(k) for k in FIELDS + ("pressure",)}
+        lo, hi = f.min_pressure, f.max_pressure
+    r = oracle.RefFluid(cfg)
+    for k, a in state.items():
+        r.upload(k, a)
+    for _ in range(20):
+        r.update(None, cfg.d_t)
+    for field in FIELDS + ("pressure",):
+        want = r.download(field)
+        assert np.array_equal(got[field], want), (field, int((got[field] != want).sum()))
+    rlo, rhi = r.pressure_range
+    r.close()
+    assert (lo, hi) == (rlo, rhi)
