@@ -1,5 +1,6 @@
-// os_resident.cuh — the whole projection phase in one cooperative launch,
-// with every tile resident in shared memory from the first sweep to the last.
+// os_resident.cuh — the whole projection (or diffusion) phase in one
+// cooperative launch, with every tile resident in shared memory from the
+// first sweep to the last.
 //
 // The pass-by-pass engine (os_blocked.cuh) restages each tile and its halo
 // from L2/HBM and relaunches for every K sweeps. Here each CTA stages its
@@ -9,8 +10,10 @@
 //   2. the CTA writes the band of owned cells within `halo` of its edges —
 //      exactly the cells that lie in its neighbours' halos — to copy X_q of
 //      (u, v), then publishes "pass q done" on its flag (release);
-//   3. it waits (acquire, bounded) until its up to 8 neighbours have
-//      published pass q, and reloads its halo ring from X_q.
+//   3. it waits (acquire, bounded) for its up to 8 neighbours to publish
+//      pass q and reloads its halo ring from X_q, part by part: each of the
+//      ring's four parts (the bands above and below, the two sides) as soon
+//      as the tiles that own it have published (ring_part_wait).
 // After the last pass it writes its whole owned tile to X_last. Every update
 // is the pass engine's, in the same order, so the result is bit-identical to
 // ceil(n/K) blocked passes, and to n per-sweep launches.
@@ -47,65 +50,6 @@ __device__ __forceinline__ void publish_flag(unsigned* flag, unsigned v) {
   if (threadIdx.x == 0) {
     asm volatile("fence.acq_rel.gpu;" ::: "memory");
     st_release_gpu(flag, v);
-  }
-}
-
-// Region cell (y, quad q) of the halo ring for flat index `it`: the top rows
-// [0, halo), the bottom rows [halo + TY, RH) (full width), then the left and
-// right quads [0, hq) and [kQuads - hq, kQuads) of the owned rows.
-__device__ __forceinline__ void ring_cell(int it, int halo, int TY, int hq, int* y, int* q) {
-  const int band = halo * kQuads;
-  if (it < band) {
-    *y = it / kQuads;
-    *q = it % kQuads;
-  } else if (it < 2 * band) {
-    it -= band;
-    *y = halo + TY + it / kQuads;
-    *q = it % kQuads;
-  } else {
-    it -= 2 * band;
-    const int side = it / (TY * hq);
-    it -= side * TY * hq;
-    *y = halo + it / hq;
-    *q = (side ? kQuads - hq : 0) + it % hq;
-  }
-}
-
-// The halo ring of u and v from global into the parity planes (the layout
-// proj_stage_in writes), all four sides in one pass so that every thread
-// keeps several loads in flight.
-template <bool PRESSURE, class S>
-__device__ __forceinline__ void reload_ring(float* smem, int RH, const S* __restrict__ u,
-                                            const S* __restrict__ v, int W, int H, int gx0,
-                                            int gy0, int halo, int TY, bool vec) {
-  const ProjPlanes P = proj_planes<PRESSURE>(smem, RH);
-  const int hq = halo / 4;
-  const int items = 2 * halo * kQuads + 2 * TY * hq;
-  for (int base = threadIdx.x; base < items; base += blockDim.x * kInFlight) {
-    float4 uq[kInFlight], vq[kInFlight];
-#pragma unroll
-    for (int r = 0; r < kInFlight; r++) {
-      const int it = base + r * blockDim.x;
-      uq[r] = vq[r] = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (it < items) {
-        int y, q;
-        ring_cell(it, halo, TY, hq, &y, &q);
-        uq[r] = load_quad_cg(u, W, H, gx0 + 4 * q, gy0 + y, vec);
-        vq[r] = load_quad_cg(v, W, H, gx0 + 4 * q, gy0 + y, vec);
-      }
-    }
-#pragma unroll
-    for (int r = 0; r < kInFlight; r++) {
-      const int it = base + r * blockDim.x;
-      if (it >= items) break;
-      int y, q;
-      ring_cell(it, halo, TY, hq, &y, &q);
-      const int s = y * kHalfW + 2 * q;
-      *reinterpret_cast<float2*>(P.ue + s) = make_float2(uq[r].x, uq[r].z);
-      *reinterpret_cast<float2*>(P.uo + s) = make_float2(uq[r].y, uq[r].w);
-      *reinterpret_cast<float2*>(P.ve + s) = make_float2(vq[r].x, vq[r].z);
-      *reinterpret_cast<float2*>(P.vo + s) = make_float2(vq[r].y, vq[r].w);
-    }
   }
 }
 
@@ -167,35 +111,6 @@ struct ResidentSync {
   int* host_err;        // mapped host word the host reads after synchronising
 };
 
-// Waits until every existing neighbour of tile (tx, ty) has published `want`.
-// Returns false when the wait gave up (here or in another CTA).
-__device__ __forceinline__ bool wait_neighbours(const ResidentSync& S, int tx, int ty,
-                                                int tiles_x, int tiles_y, unsigned want) {
-  __shared__ int give_up;
-  if (threadIdx.x == 0) give_up = 0;
-  __syncthreads();
-  if (threadIdx.x < 9 && threadIdx.x != 4) {
-    const int nx = tx + (int)(threadIdx.x % 3) - 1, ny = ty + (int)(threadIdx.x / 3) - 1;
-    if (nx >= 0 && nx < tiles_x && ny >= 0 && ny < tiles_y) {
-      const unsigned* f = S.flags + ny * tiles_x + nx;
-      for (int it = 0; (int)(ld_acquire_gpu(f) - want) < 0; it++) {
-        if (it >= kSpinLimit || (it % 64 == 63 && *(volatile int*)S.dev_err)) {
-          if (atomicCAS(S.dev_err, 0, 1) == 0) {
-            *(volatile int*)S.host_err = 1;
-            __threadfence_system();
-          }
-          give_up = 1;
-          break;
-        }
-        __nanosleep(32);
-      }
-    }
-  }
-  // The acquire loads order the reloads that follow the barrier.
-  __syncthreads();
-  return give_up == 0;
-}
-
 // Part `part` of the halo ring: 0 the region rows [0, halo) (owned by the
 // tiles one row down, ty - 1), 1 the rows [halo + TY, RH) (the tiles one row
 // up), 2 the left quads [0, hq) of the owned rows (the tile on the left),
@@ -214,22 +129,21 @@ __device__ __forceinline__ void ring_part_cell(int part, int it, int halo, int T
   }
 }
 
-// The halo exchange's wait and reload, part by part: each part of the ring
-// is reloaded as soon as the tiles that own it have published, instead of
-// the whole ring after all eight neighbours have. The warps are split among
-// the four parts about in proportion to their sizes (3/8 to each band, 1/8
-// to each side); each part's first warp polls its neighbours' flags (three
-// for a band, one for a side, with the same bounded wait as
-// wait_neighbours) and the part's warps meet at a named barrier of their
-// own before they load, so the acquire loads order their reloads. Ends with
-// a barrier of the whole CTA; returns false, in every thread, when a wait
-// gave up here or in another CTA (the reloaded ring is then not used).
-template <bool PRESSURE, class S>
-__device__ __forceinline__ bool exchange_ring(const ResidentSync& sync, float* smem, int RH,
-                                              const S* __restrict__ u, const S* __restrict__ v,
-                                              int W, int H, int gx0, int gy0, int halo, int TY,
-                                              bool vec, int tx, int ty, int tiles_x, int tiles_y,
-                                              unsigned want) {
+// The wait of a halo exchange, part by part: each part of the ring is
+// reloaded as soon as the tiles that own it have published, instead of the
+// whole ring after all eight neighbours have. The warps are split among the
+// four parts about in proportion to their sizes (3/8 to each band, 1/8 to
+// each side); each part's first warp polls its neighbours' flags (three for
+// a band, one for a side, with the same bounded wait as wait_neighbours)
+// and the part's warps meet at a named barrier of their own, so the acquire
+// loads order the reloads that follow. On return *part is this thread's
+// part, and the thread reloads the part's cells t0, t0 + stride, ...; the
+// result is the CTA's give-up word, which the caller reads after the
+// barrier that ends the reload (non-zero: a wait gave up, here or in
+// another CTA, and the ring is not to be used).
+__device__ __forceinline__ volatile int* ring_part_wait(const ResidentSync& sync, int tx, int ty,
+                                                        int tiles_x, int tiles_y, unsigned want,
+                                                        int* part_out, int* t0, int* stride) {
   __shared__ int give_up;
   if (threadIdx.x == 0) give_up = 0;
   __syncthreads();
@@ -265,11 +179,27 @@ __device__ __forceinline__ bool exchange_ring(const ResidentSync& sync, float* s
   }
   __syncwarp();
   asm volatile("bar.sync %0, %1;" ::"r"(1 + part), "r"(wn * 32) : "memory");
-  if (!*(volatile int*)&give_up) {
+  *part_out = part;
+  *t0 = threadIdx.x - w0 * 32;
+  *stride = wn * 32;
+  return &give_up;
+}
+
+// The projection's exchange: the ring of u and v into the parity planes,
+// part by part (ring_part_wait). Ends with a barrier of the whole CTA;
+// returns false, in every thread, when a wait gave up.
+template <bool PRESSURE, class S>
+__device__ __forceinline__ bool exchange_ring(const ResidentSync& sync, float* smem, int RH,
+                                              const S* __restrict__ u, const S* __restrict__ v,
+                                              int W, int H, int gx0, int gy0, int halo, int TY,
+                                              bool vec, int tx, int ty, int tiles_x, int tiles_y,
+                                              unsigned want) {
+  int part, t0, stride;
+  volatile int* give_up = ring_part_wait(sync, tx, ty, tiles_x, tiles_y, want, &part, &t0, &stride);
+  if (!*give_up) {
     const ProjPlanes P = proj_planes<PRESSURE>(smem, RH);
     const int hq = halo / 4;
     const int items = ring_part_items(part, halo, TY, hq);
-    const int t0 = threadIdx.x - w0 * 32, stride = wn * 32;
     for (int base = t0; base < items; base += stride * kInFlight) {
       float4 uq[kInFlight], vq[kInFlight];
 #pragma unroll
@@ -298,7 +228,47 @@ __device__ __forceinline__ bool exchange_ring(const ResidentSync& sync, float* s
     }
   }
   __syncthreads();
-  return *(volatile int*)&give_up == 0;
+  return *give_up == 0;
+}
+
+// The diffusion's exchange: the ring of u into the dense region A, part by
+// part (ring_part_wait). Ends with a barrier; returns false, in every
+// thread, when a wait gave up.
+template <class S>
+__device__ __forceinline__ bool exchange_ring_dense(const ResidentSync& sync, float* A,
+                                                    const S* __restrict__ u, int W, int H,
+                                                    int gx0, int gy0, int halo, int TY, bool vec,
+                                                    int tx, int ty, int tiles_x, int tiles_y,
+                                                    unsigned want) {
+  int part, t0, stride;
+  volatile int* give_up = ring_part_wait(sync, tx, ty, tiles_x, tiles_y, want, &part, &t0, &stride);
+  if (!*give_up) {
+    const int hq = halo / 4;
+    const int items = ring_part_items(part, halo, TY, hq);
+    for (int base = t0; base < items; base += stride * kInFlight) {
+      float4 uq[kInFlight];
+#pragma unroll
+      for (int r = 0; r < kInFlight; r++) {
+        const int it = base + r * stride;
+        uq[r] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (it < items) {
+          int y, q;
+          ring_part_cell(part, it, halo, TY, hq, &y, &q);
+          uq[r] = load_quad_cg(u, W, H, gx0 + 4 * q, gy0 + y, vec);
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < kInFlight; r++) {
+        const int it = base + r * stride;
+        if (it >= items) break;
+        int y, q;
+        ring_part_cell(part, it, halo, TY, hq, &y, &q);
+        *reinterpret_cast<float4*>(A + y * kRegionW + 4 * q) = uq[r];
+      }
+    }
+  }
+  __syncthreads();
+  return *give_up == 0;
 }
 
 template <bool PRESSURE, class S>
@@ -353,34 +323,6 @@ k_project_resident(S* U0, S* U1, S* V0, S* V1, int cu, int cv, float* __restrict
 // sweep updates (domain boundary, off the grid) are constant and staged into
 // both buffers at the start.
 // ---------------------------------------------------------------------------
-
-template <class S>
-__device__ __forceinline__ void reload_ring_dense(float* A, const S* __restrict__ u, int W, int H,
-                                                  int gx0, int gy0, int halo, int TY, bool vec) {
-  const int hq = halo / 4;
-  const int items = 2 * halo * kQuads + 2 * TY * hq;
-  for (int base = threadIdx.x; base < items; base += blockDim.x * kInFlight) {
-    float4 uq[kInFlight];
-#pragma unroll
-    for (int r = 0; r < kInFlight; r++) {
-      const int it = base + r * blockDim.x;
-      uq[r] = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (it < items) {
-        int y, q;
-        ring_cell(it, halo, TY, hq, &y, &q);
-        uq[r] = load_quad_cg(u, W, H, gx0 + 4 * q, gy0 + y, vec);
-      }
-    }
-#pragma unroll
-    for (int r = 0; r < kInFlight; r++) {
-      const int it = base + r * blockDim.x;
-      if (it >= items) break;
-      int y, q;
-      ring_cell(it, halo, TY, hq, &y, &q);
-      *reinterpret_cast<float4*>(A + y * kRegionW + 4 * q) = uq[r];
-    }
-  }
-}
 
 // Owned cells within `halo` of the tile's edges, from A to global.
 template <class S>
@@ -446,17 +388,21 @@ k_diffuse_resident(S* U0, S* U1, int cu, Consts c, const StepParams* __restrict_
     }
     publish_band_dense<S>(A, uo, W, H, gx0, gy0, halo, TX, TY, vec);
     publish_flag(sync.flags + blockIdx.x, epoch + q + 1);
-    if (!wait_neighbours(sync, tx, ty, tiles_x, tiles_y, epoch + q + 1)) return;
+    // Owned cells rounded as the pass engine's write-back would round them
+    // (disjoint from the ring), then the ring, part by part.
     round_owned_dense<S>(A, halo, TX, TY);
-    reload_ring_dense<S>(A, uo, W, H, gx0, gy0, halo, TY, vec);
-    __syncthreads();
+    if (!exchange_ring_dense<S>(sync, A, uo, W, H, gx0, gy0, halo, TY, vec, tx, ty, tiles_x,
+                                tiles_y, epoch + q + 1))
+      return;
   }
 }
 
 // Failure-detection self-test: tile 0 of a 2 x 1 grid waits for tile 1,
 // which no CTA runs, so the wait must give up and report.
 __global__ void k_wait_selftest(ResidentSync sync) {
-  wait_neighbours(sync, 0, 0, 2, 1, 1u);
+  int part, t0, stride;
+  ring_part_wait(sync, 0, 0, 2, 1, 1u, &part, &t0, &stride);
+  __syncthreads();
 }
 
 // Host: tile geometry for K sweeps per exchange (halo 2K), with at most one
