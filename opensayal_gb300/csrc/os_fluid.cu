@@ -1516,36 +1516,58 @@ TuneChoice autotune_projection(const os_config& base) {
     }
   }
   const float dt = base.d_t > 0.0f ? base.d_t : 0.05f;
-  TuneChoice best = kDefault;
-  float best_ms = 0.0f;
-  auto try_choice = [&](const TuneChoice& cand) {
+  // ms per step of a candidate over `steps` steps, or 0 when the grid does
+  // not take that form.
+  auto time_choice = [&](const TuneChoice& cand, int steps) -> float {
     os_config c = base;
     c.projection_block = cand.K;
     c.projection_resident = cand.resident ? cand.resident : -1;
     os_handle* t = nullptr;
-    if (os_create(&c, &t) != OS_OK) return;  // e.g. out of memory: skip
+    if (os_create(&c, &t) != OS_OK) return 0.0f;  // e.g. out of memory: skip
     const int got = (t->resident ? 1 : 0) | (t->resident_diff ? 2 : 0);
     if (got != cand.resident) {  // the grid does not fit that form
       os_destroy(t);
-      return;
+      return 0.0f;
     }
     if (cand.diff_k > 0) t->diff_k = cand.diff_k;  // before the first step captures the graph
-    const float ms = time_steps(t, dt, 3, 12);
+    const float ms = time_steps(t, dt, 3, steps);
     os_destroy(t);
+    return ms;
+  };
+  // Two rounds: 12 steps of every candidate, then 60 steps of the three
+  // fastest, since forms within a percent of each other are told apart only
+  // by longer timings.
+  std::vector<std::pair<float, TuneChoice>> timed;
+  for (const TuneChoice& cand : cands)
+    if (cand.K <= std::max(1, base.projection_n)) {
+      const float ms = time_choice(cand, 12);
+      if (ms > 0.0f) timed.push_back({ms, cand});
+    }
+  std::sort(timed.begin(), timed.end(),
+            [](const auto& a, const auto& b) { return a.first < b.first; });
+  TuneChoice best = kDefault;
+  float best_ms = 0.0f;
+  for (size_t r = 0; r < timed.size() && r < 3; r++) {
+    const float ms = time_choice(timed[r].second, 60);
     if (ms > 0.0f && (best_ms == 0.0f || ms < best_ms)) {
       best_ms = ms;
-      best = cand;
+      best = timed[r].second;
     }
-  };
-  for (const TuneChoice& cand : cands)
-    if (cand.K <= std::max(1, base.projection_n)) try_choice(cand);
+  }
   // Deeper diffusion passes than the projection's (the Jacobi halo is half
   // the red/black one), when the diffusion runs pass by pass.
   if (base.viscosity != 0.0f && base.diffusion_block == 0 && best_ms > 0.0f &&
       !(best.resident & 2)) {
     const TuneChoice chosen = best;
     for (int dk : {12, 16, 20})
-      if (dk > chosen.K && dk <= base.projection_n) try_choice({chosen.K, chosen.resident, dk});
+      if (dk > chosen.K && dk <= base.projection_n) {
+        const TuneChoice cand{chosen.K, chosen.resident, dk};
+        const float ms = time_choice(cand, 60);
+        if (ms > 0.0f && ms < best_ms) {
+          best_ms = ms;
+          best = cand;
+        }
+      }
   }
   g_err[0] = '\0';  // a candidate that failed is not the caller's error
   std::lock_guard<std::mutex> lock(g_tune_mu);
