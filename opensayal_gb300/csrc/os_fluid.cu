@@ -848,6 +848,19 @@ static int create_handle(const os_config* cfg, Arena* arena, os_handle** out) {
   cudaError_t e = cudaSetDevice(cfg->device);
   if (e != cudaSuccess)
     return fail(set_err(OS_ERR_CUDA, "cudaSetDevice(%d): %s", cfg->device, cudaGetErrorString(e)));
+  // The depth and form are chosen before this handle allocates anything, so
+  // that the trial handles never share the device with it.
+  int resident = cfg->projection_resident > 0 ? cfg->projection_resident : 0;
+  if (h->block_k == 0) {
+    if (h->storage == OS_STORAGE_F64) {
+      h->block_k = -1;
+    } else {
+      const TuneChoice t = autotune_projection(*cfg);
+      h->block_k = t.K;
+      if (t.diff_k > 0) h->diff_k = t.diff_k;
+      resident = t.resident;
+    }
+  }
   if (arena) {
     h->arena = arena;
     h->arena_size = handle_footprint(*cfg);
@@ -900,17 +913,6 @@ static int create_handle(const os_config* cfg, Arena* arena, os_handle** out) {
   if ((e = cudaGetLastError()) != cudaSuccess ||
       (e = cudaStreamSynchronize(h->stream)) != cudaSuccess)
     return fail(set_err(OS_ERR_CUDA, "init: %s", cudaGetErrorString(e)));
-  int resident = cfg->projection_resident > 0 ? cfg->projection_resident : 0;
-  if (h->block_k == 0) {
-    if (h->storage == OS_STORAGE_F64) {
-      h->block_k = -1;
-    } else {
-      const TuneChoice t = autotune_projection(*cfg);
-      h->block_k = t.K;
-      if (t.diff_k > 0) h->diff_k = t.diff_k;
-      resident = t.resident;
-    }
-  }
   if (resident) {
     const int rc = enable_resident(h, resident);
     if (rc) return fail(rc);
