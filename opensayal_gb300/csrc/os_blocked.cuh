@@ -407,8 +407,10 @@ __device__ __forceinline__ void proj_sweeps(float* smem, const Consts& c,
 // ---------------------------------------------------------------------------
 // The same sweeps with the vertical faces in registers.
 //
-// Thread t owns the column pair (2p, 2p + 1), p = t % 128, over the R rows
-// [y0, y0 + R) of strip s = t / 128, y0 = s * R. R is even, so every strip
+// Thread t owns the column pair (2p, 2p + 1) over the R rows [y0, y0 + R) of
+// strip s = t / 128, y0 = s * R; the 128 threads of a strip cover p = 0 .. 127
+// (in column blocks of 32 rotated by the strip, see proj_sweeps_vreg). R is
+// even, so every strip
 // starts on an even row and the active column of the pair in row y0 + r is
 // (r + colour) & 1 for every thread: fixed once the row loop is unrolled. The
 // thread's faces v(x, y0 .. y0 + R - 1) stay in registers for all the sweeps of
@@ -425,6 +427,13 @@ __device__ __forceinline__ void proj_sweeps(float* smem, const Consts& c,
 // that side then writes the new value to the face's own word in the v plane;
 // after the barrier the other side reads it. The word is next written by the
 // side that just read it, so one barrier per half-sweep suffices.
+//
+// Most cells have four fluid neighbours. A warp whose cells the half-sweep
+// needs are all such cells runs a loop of its own without flag loads, flag
+// tests or the division by the neighbour count (vreg_half_sweep); measured on
+// the 1920 x 1080 tunnel, that took a pass of 8 sweeps from 22.9 to 17.0 us
+// on the tiles without walls, the obstacle or cells off the grid, and to
+// 20.2-20.8 us on the others, where a quarter of the warps still test flags.
 // ---------------------------------------------------------------------------
 // project_faces without branches and without the pressure, for cells taken
 // two rows at a time: `f` is the sweep flag byte, 0 for any cell not updated
@@ -439,6 +448,23 @@ __device__ __forceinline__ void project_faces_sel(uint32_t f, const Consts& c, f
   if (f & F_RIGHT) right_u = right_u - velocity_diff;
   if (f & F_BOTTOM) vc = vc + velocity_diff;
   if (f & F_TOP) top_v = top_v - velocity_diff;
+}
+
+// The sweep flag of an active cell whose four neighbours are all fluid.
+constexpr uint32_t kFullFlag = 1u | F_NBR_MASK | (4u << kSweepCountShift);
+
+// project_faces_sel for a cell with flag kFullFlag: every face is updated,
+// and s = 4. The division by 4 is the product by 0.25, which gives the bits
+// of the fast-math division by a runtime 4 for every float input (all 2^32
+// patterns compared by tests/cpp/quarter_division.cu).
+__device__ __forceinline__ void project_faces_full(const Consts& c, float& uc, float& right_u,
+                                                   float& vc, float& top_v) {
+  const float divergence = right_u - uc + top_v - vc;
+  const float velocity_diff = mul_rn(c.o, mul_rn(divergence, 0.25f));
+  uc = uc + velocity_diff;
+  right_u = right_u - velocity_diff;
+  vc = vc + velocity_diff;
+  top_v = top_v - velocity_diff;
 }
 
 // One row of a half-sweep, with branches (the accumulated pressure needs the
@@ -472,10 +498,23 @@ __device__ __forceinline__ void vreg_row(const ProjPlanes& P, float (&v)[2][R], 
 // single such row, or a column off the cone, is predicated off. An inactive
 // cell in the cone stores its faces unchanged (no other cell of the colour
 // touches them).
+//
+// Bit r of `full` (the same in every lane of the warp) says that the active
+// cell of row r has flag kFullFlag in every lane. When both rows of every
+// pair the half-sweep needs are full, the warp takes project_faces_full
+// without reading or testing flags, and without the cone: a cell off the
+// cone is updated too. That is harmless,
+// since the cone shrinks by one cell per side each half-sweep: the faces of
+// a cell off the cone belong to it and to its neighbours, which are off the
+// cone from the next half-sweep on, so what it writes never reaches a cell
+// in the cone or an owned face. Only the cell in column kRegionW - 1 (the odd
+// column of the last thread) has a face outside the region, u(kRegionW), and
+// that face is never stored.
 template <int COLOUR, bool PRESSURE, int R>
 __device__ __forceinline__ void vreg_half_sweep(const ProjPlanes& P, float (&v)[2][R],
                                                 float (&vt)[2], int p, int y0, int RH, int halo,
-                                                int reach, const Consts& c, float d_t) {
+                                                int reach, const Consts& c, float d_t,
+                                                uint32_t full) {
   const int lo = max(0, halo - 1 - reach);      // first needed cell, both axes
   const int y_end = min(RH - 1, RH - halo + reach);
   const int x_end = kRegionW - halo + reach;    // at most 255: u(x + 1) stays in the row
@@ -483,40 +522,71 @@ __device__ __forceinline__ void vreg_half_sweep(const ProjPlanes& P, float (&v)[
   const uint32_t rows = ((1u << rhi) - 1u) & ~((1u << rlo) - 1u);
   const bool col_ok[2] = {2 * p >= lo && 2 * p < x_end, 2 * p + 1 >= lo && 2 * p + 1 < x_end};
   constexpr int ca = COLOUR & 1, cb = ca ^ 1;   // active columns of even and odd rows
-  // Rows whose active cell of this thread's pair is in the cone.
-  const uint32_t live = rows & ((col_ok[ca] ? 0x55555555u : 0u) | (col_ok[cb] ? 0xaaaaaaaau : 0u));
+  // Row pairs with a row in the cone, and row pairs whose two rows are full
+  // (bit r of each, r even); both masks are the same in every lane.
+  const uint32_t pairs = (rows | (rows >> 1)) & 0x55555555u;
+  const uint32_t pairs_full = full & (full >> 1) & 0x55555555u;
+  if (!PRESSURE && (pairs & ~pairs_full) == 0u) {
+    // Every pair the half-sweep needs is full: a loop of its own, so that
+    // the warps on it run a short stretch of code.
+    const bool edge = p == kHalfW - 1;
 #pragma unroll
-  for (int r = 0; r < R; r += 2) {
-    if (((rows >> r) & 3u) == 0u) continue;  // both rows off the cone: the same for the warp
-    const bool ia = (live >> r) & 1u;
-    const bool ib = (live >> (r + 1)) & 1u;
-    if constexpr (PRESSURE) {
-      vreg_row<ca, PRESSURE, R>(P, v, vt, p, y0, r, ia, c, d_t);
-      vreg_row<cb, PRESSURE, R>(P, v, vt, p, y0, r + 1, ib, c, d_t);
-      continue;
-    }
-    const int ea = (y0 + r) * kHalfW + p, eb = ea + kHalfW;
-    float* uLa = (ca ? P.uo : P.ue) + ea;
-    float* uRa = ca ? P.ue + ea + 1 : P.uo + ea;
-    float* uLb = (cb ? P.uo : P.ue) + eb;
-    float* uRb = cb ? P.ue + eb + 1 : P.uo + eb;
-    // Both rows of a pair that is not skipped lie inside the region (the cone
-    // ends below row RH - 1), so the loads need no predicate; only the updates
-    // and the stores do.
-    const uint32_t fa = ia ? (uint32_t)(ca ? P.fo : P.fe)[ea] : 0u;
-    const uint32_t fb = ib ? (uint32_t)(cb ? P.fo : P.fe)[eb] : 0u;
-    float a0 = *uLa, a1 = *uRa;
-    float b0 = *uLb, b1 = *uRb;
-    float& top_b = (r + 2 < R) ? v[cb][r + 2] : vt[cb];
-    project_faces_sel(fa, c, a0, a1, v[ca][r], v[ca][r + 1]);
-    project_faces_sel(fb, c, b0, b1, v[cb][r + 1], top_b);
-    if (ia) {
+    for (int r = 0; r < R; r += 2) {
+      if (((pairs >> r) & 1u) == 0u) continue;
+      // Both rows lie below the region's top row (the flags say so), so
+      // every load is inside the region.
+      const int ea = (y0 + r) * kHalfW + p, eb = ea + kHalfW;
+      float* uLa = (ca ? P.uo : P.ue) + ea;
+      float* uRa = ca ? P.ue + ea + 1 : P.uo + ea;
+      float* uLb = (cb ? P.uo : P.ue) + eb;
+      float* uRb = cb ? P.ue + eb + 1 : P.uo + eb;
+      float a0 = *uLa, a1 = *uRa;
+      float b0 = *uLb, b1 = *uRb;
+      float& top_b = (r + 2 < R) ? v[cb][r + 2] : vt[cb];
+      project_faces_full(c, a0, a1, v[ca][r], v[ca][r + 1]);
+      project_faces_full(c, b0, b1, v[cb][r + 1], top_b);
       *uLa = a0;
-      *uRa = a1;
-    }
-    if (ib) {
+      if (!(ca && edge)) *uRa = a1;
       *uLb = b0;
-      *uRb = b1;
+      if (!(cb && edge)) *uRb = b1;
+    }
+  } else {
+    // Rows whose active cell of this thread's pair is in the cone.
+    const uint32_t live =
+        rows & ((col_ok[ca] ? 0x55555555u : 0u) | (col_ok[cb] ? 0xaaaaaaaau : 0u));
+#pragma unroll
+    for (int r = 0; r < R; r += 2) {
+      if (((rows >> r) & 3u) == 0u) continue;  // both rows off the cone: the same for the warp
+      const bool ia = (live >> r) & 1u;
+      const bool ib = (live >> (r + 1)) & 1u;
+      if constexpr (PRESSURE) {
+        vreg_row<ca, PRESSURE, R>(P, v, vt, p, y0, r, ia, c, d_t);
+        vreg_row<cb, PRESSURE, R>(P, v, vt, p, y0, r + 1, ib, c, d_t);
+        continue;
+      }
+      const int ea = (y0 + r) * kHalfW + p, eb = ea + kHalfW;
+      float* uLa = (ca ? P.uo : P.ue) + ea;
+      float* uRa = ca ? P.ue + ea + 1 : P.uo + ea;
+      float* uLb = (cb ? P.uo : P.ue) + eb;
+      float* uRb = cb ? P.ue + eb + 1 : P.uo + eb;
+      // Both rows of a pair that is not skipped lie inside the region (the
+      // cone ends below row RH - 1), so the loads need no predicate; only the
+      // updates and the stores do.
+      const uint32_t fa = ia ? (uint32_t)(ca ? P.fo : P.fe)[ea] : 0u;
+      const uint32_t fb = ib ? (uint32_t)(cb ? P.fo : P.fe)[eb] : 0u;
+      float a0 = *uLa, a1 = *uRa;
+      float b0 = *uLb, b1 = *uRb;
+      float& top_b = (r + 2 < R) ? v[cb][r + 2] : vt[cb];
+      project_faces_sel(fa, c, a0, a1, v[ca][r], v[ca][r + 1]);
+      project_faces_sel(fb, c, b0, b1, v[cb][r + 1], top_b);
+      if (ia) {
+        *uLa = a0;
+        *uRa = a1;
+      }
+      if (ib) {
+        *uLb = b0;
+        *uRb = b1;
+      }
     }
   }
   // Boundary faces this half-sweep may have changed, for the neighbouring strip.
@@ -547,8 +617,13 @@ __device__ __noinline__ void proj_sweeps_vreg(const Consts c, float d_t, int swe
   extern __shared__ __align__(16) float dyn_smem[];
   const int RH = TY + 2 * halo;
   const ProjPlanes P = proj_planes<PRESSURE>(dyn_smem, RH);
-  const int p = threadIdx.x % kHalfW;
-  const int y0 = (threadIdx.x / kHalfW) * R;
+  // Strip s's four warps take the column blocks (w + s) mod 4, so that the
+  // warps each scheduler partition holds (warp w of every strip) cover every
+  // block: the rows that need the flag-driven path (walls, the obstacle,
+  // cells off the grid) do not all fall to one partition.
+  const int strip = threadIdx.x / kHalfW;
+  const int p = ((((threadIdx.x >> 5) + strip) & (kHalfW / 32 - 1)) << 5) | (threadIdx.x & 31);
+  const int y0 = strip * R;
   float v[2][R], vt[2];
 #pragma unroll
   for (int r = 0; r < R; r++) {
@@ -560,14 +635,31 @@ __device__ __noinline__ void proj_sweeps_vreg(const Consts c, float d_t, int swe
   const bool top_in = y0 + R < RH;
   vt[0] = top_in ? P.ve[(y0 + R) * kHalfW + p] : 0.0f;
   vt[1] = top_in ? P.vo[(y0 + R) * kHalfW + p] : 0.0f;
+  // Per colour, the rows whose active cell has flag kFullFlag in every lane
+  // of the warp (rows from the region's top row on never do; the warp's
+  // lanes share y0). The flags do not change during the sweeps.
+  uint32_t full[2] = {0u, 0u};
+  if (!PRESSURE) {
+#pragma unroll
+    for (int colour = 0; colour < 2; colour++) {
+      uint32_t m = 0u;
+#pragma unroll
+      for (int r = 0; r < R; r++) {
+        const int y = y0 + r;
+        const uint8_t* F = ((r + colour) & 1) ? P.fo : P.fe;
+        if (y < RH - 1 && F[y * kHalfW + p] == kFullFlag) m |= 1u << r;
+      }
+      full[colour] = __reduce_and_sync(0xffffffffu, m);
+    }
+  }
   // Every thread has its copies before any boundary word is rewritten.
   __syncthreads();
   for (int t = 0; t < sweeps; t++) {
     const int reach = 2 * (sweeps - t) - 1;  // half-sweeps after the even one
-    vreg_half_sweep<0, PRESSURE, R>(P, v, vt, p, y0, RH, halo, reach, c, d_t);
+    vreg_half_sweep<0, PRESSURE, R>(P, v, vt, p, y0, RH, halo, reach, c, d_t, full[0]);
     __syncthreads();
     vreg_receive<0, R>(P, v, vt, p, y0, RH);
-    vreg_half_sweep<1, PRESSURE, R>(P, v, vt, p, y0, RH, halo, reach - 1, c, d_t);
+    vreg_half_sweep<1, PRESSURE, R>(P, v, vt, p, y0, RH, halo, reach - 1, c, d_t, full[1]);
     __syncthreads();
     vreg_receive<1, R>(P, v, vt, p, y0, RH);
   }
