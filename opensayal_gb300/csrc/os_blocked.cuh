@@ -493,23 +493,24 @@ __device__ __forceinline__ void vreg_row(const ProjPlanes& P, float (&v)[2][R], 
 // two active cells sit in different columns and share no face): both rows'
 // loads first, then both updates, then both stores, with no branches, so the
 // two dependency chains overlap (with the pressure on, each row on its own,
-// vreg_row). A pair of rows wholly outside the cone or
-// the region is skipped (a branch that is the same for the whole warp); a
-// single such row, or a column off the cone, is predicated off. An inactive
-// cell in the cone stores its faces unchanged (no other cell of the colour
-// touches them).
+// vreg_row). A pair of rows wholly outside the cone or the region is skipped
+// (a branch that is the same for the whole warp). An inactive cell stores
+// its faces unchanged (no other cell of the colour touches them).
+//
+// Within a pair that is not skipped, a cell off the cone is updated like the
+// others. That is harmless, since the cone shrinks by one cell per side each
+// half-sweep: the faces of a cell off the cone belong to it and to its
+// neighbours, which are off the cone from the next half-sweep on, so what it
+// writes never reaches a cell in the cone or an owned face. Only the cell in
+// column kRegionW - 1 (the odd column of the last thread) has a face in
+// shared memory outside the region, u(kRegionW), and that face is never
+// stored; the top face of row RH - 1 is a register that is never stored or
+// passed to another strip. With the pressure on the cone is kept per cell.
 //
 // Bit r of `full` (the same in every lane of the warp) says that the active
 // cell of row r has flag kFullFlag in every lane. When both rows of every
 // pair the half-sweep needs are full, the warp takes project_faces_full
-// without reading or testing flags, and without the cone: a cell off the
-// cone is updated too. That is harmless,
-// since the cone shrinks by one cell per side each half-sweep: the faces of
-// a cell off the cone belong to it and to its neighbours, which are off the
-// cone from the next half-sweep on, so what it writes never reaches a cell
-// in the cone or an owned face. Only the cell in column kRegionW - 1 (the odd
-// column of the last thread) has a face outside the region, u(kRegionW), and
-// that face is never stored.
+// without reading or testing flags.
 template <int COLOUR, bool PRESSURE, int R>
 __device__ __forceinline__ void vreg_half_sweep(const ProjPlanes& P, float (&v)[2][R],
                                                 float (&vt)[2], int p, int y0, int RH, int halo,
@@ -551,17 +552,15 @@ __device__ __forceinline__ void vreg_half_sweep(const ProjPlanes& P, float (&v)[
       if (!(cb && edge)) *uRb = b1;
     }
   } else {
-    // Rows whose active cell of this thread's pair is in the cone.
-    const uint32_t live =
-        rows & ((col_ok[ca] ? 0x55555555u : 0u) | (col_ok[cb] ? 0xaaaaaaaau : 0u));
+    const bool edge = p == kHalfW - 1;
 #pragma unroll
     for (int r = 0; r < R; r += 2) {
       if (((rows >> r) & 3u) == 0u) continue;  // both rows off the cone: the same for the warp
-      const bool ia = (live >> r) & 1u;
-      const bool ib = (live >> (r + 1)) & 1u;
       if constexpr (PRESSURE) {
-        vreg_row<ca, PRESSURE, R>(P, v, vt, p, y0, r, ia, c, d_t);
-        vreg_row<cb, PRESSURE, R>(P, v, vt, p, y0, r + 1, ib, c, d_t);
+        const uint32_t live =
+            rows & ((col_ok[ca] ? 0x55555555u : 0u) | (col_ok[cb] ? 0xaaaaaaaau : 0u));
+        vreg_row<ca, PRESSURE, R>(P, v, vt, p, y0, r, (live >> r) & 1u, c, d_t);
+        vreg_row<cb, PRESSURE, R>(P, v, vt, p, y0, r + 1, (live >> (r + 1)) & 1u, c, d_t);
         continue;
       }
       const int ea = (y0 + r) * kHalfW + p, eb = ea + kHalfW;
@@ -569,24 +568,17 @@ __device__ __forceinline__ void vreg_half_sweep(const ProjPlanes& P, float (&v)[
       float* uRa = ca ? P.ue + ea + 1 : P.uo + ea;
       float* uLb = (cb ? P.uo : P.ue) + eb;
       float* uRb = cb ? P.ue + eb + 1 : P.uo + eb;
-      // Both rows of a pair that is not skipped lie inside the region (the
-      // cone ends below row RH - 1), so the loads need no predicate; only the
-      // updates and the stores do.
-      const uint32_t fa = ia ? (uint32_t)(ca ? P.fo : P.fe)[ea] : 0u;
-      const uint32_t fb = ib ? (uint32_t)(cb ? P.fo : P.fe)[eb] : 0u;
+      const uint32_t fa = (ca ? P.fo : P.fe)[ea];
+      const uint32_t fb = (cb ? P.fo : P.fe)[eb];
       float a0 = *uLa, a1 = *uRa;
       float b0 = *uLb, b1 = *uRb;
       float& top_b = (r + 2 < R) ? v[cb][r + 2] : vt[cb];
       project_faces_sel(fa, c, a0, a1, v[ca][r], v[ca][r + 1]);
       project_faces_sel(fb, c, b0, b1, v[cb][r + 1], top_b);
-      if (ia) {
-        *uLa = a0;
-        *uRa = a1;
-      }
-      if (ib) {
-        *uLb = b0;
-        *uRb = b1;
-      }
+      *uLa = a0;
+      if (!(ca && edge)) *uRa = a1;
+      *uLb = b0;
+      if (!(cb && edge)) *uRb = b1;
     }
   }
   // Boundary faces this half-sweep may have changed, for the neighbouring strip.
