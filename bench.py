@@ -340,29 +340,34 @@ def run_gb300(args, world, rank, local) -> dict | None:
                            "how": "os_update (synchronous) then os_download of the smoke, "
                                   "every step, as the reference's frame loop does"}}
 
-    # roofline of the dominant phase (projection), timed alone on the same stream
+    # roofline of the dominant phase (projection), timed alone on the same
+    # stream: CUDA events around the phase's own kernels, as the step runs
+    # them (a phase called on its own also copies the velocity back to the
+    # public fields when its pass count leaves it in the other buffers; that
+    # copy is timed apart and left out)
     pk = peaks()
-    proj_ms, proj_kernels = f.profile_phase(native.PHASE_PROJECTION, None, dt, 3, sptr)
-    proj_s = proj_ms / 3 / 1e3
+    proj_kms, proj_ms, proj_kernels = f.profile_phase_kernels(native.PHASE_PROJECTION, None, dt,
+                                                              3, sptr)
+    proj_s = proj_kms / 3 / 1e3
     proj_bytes = 17 * cfg.projection_n * cells
-    diff_ms, diff_kernels = f.profile_phase(native.PHASE_DIFFUSION, None, dt, 3, sptr)
+    diff_kms, diff_ms, diff_kernels = f.profile_phase_kernels(native.PHASE_DIFFUSION, None, dt,
+                                                              3, sptr)
     achieved = proj_bytes / proj_s / 1e9
     # DRAM bytes of the projection phase: per launch from the ncu capture
     # summarised in profiles/ (same workload and blocking depth) or scaled
     # from one, as the entry says, times the phase's launches; null when the
     # configuration was not captured.
     traffic, traffic_source, on_chip = None, "not captured for this configuration", None
+    # launches of the projection kernel in one phase: one resident launch, or
+    # one blocked launch per pass
+    k_proj = (1 if f.fields().projection_resident else
+              -(-cfg.projection_n // max(1, f.fields().projection_block)))
     tfile = ROOT / "profiles" / "roofline_traffic.json"
     if tfile.exists():
         key = f"{args.workload}:block{f.fields().projection_block}" + (
             ":resident" if f.fields().projection_resident else "")
         entry = json.loads(tfile.read_text()).get(key)
         if entry:
-            # launches of the projection kernel in one phase: one resident
-            # launch, or one blocked launch per pass (the phase timed alone
-            # also copies the result back, which the step does not)
-            k_proj = (1 if f.fields().projection_resident else
-                      -(-cfg.projection_n // max(1, f.fields().projection_block)))
             traffic = entry["bytes_per_launch"] * k_proj
             traffic_source = entry["source"]
             if "smsp__issue_active" in entry:
@@ -388,7 +393,9 @@ def run_gb300(args, world, rank, local) -> dict | None:
                      "unit": "GB/s", "frac": achieved / pk["hbm_gbs"], "traffic": traffic,
                      "traffic_source": traffic_source,
                      "kernel": "projection phase (17 B/cell per red/black sweep x n sweeps)",
-                     "kernels_per_phase_timed": proj_kernels // 3, "peak_source": pk["source"]},
+                     "kernels_per_phase_timed": k_proj,
+                     "launches_per_phase_with_copy_back": proj_kernels // 3,
+                     "peak_source": pk["source"]},
         # The projection's sweeps run in shared memory and its halo exchanges
         # go through L2; DRAM sees the fields about once per phase. The level
         # that binds is on-chip, so the same algorithmic rate is also given
@@ -401,7 +408,11 @@ def run_gb300(args, world, rank, local) -> dict | None:
         "step_roofline": {"bytes_per_cell_step": step_bytes,
                           "achieved": step_bytes * value / world / 1e9, "unit": "GB/s",
                           "frac": step_bytes * value / world / 1e9 / pk["hbm_gbs"]},
-        "phase_ms": {"projection": proj_ms / 3, "diffusion": diff_ms / 3},
+        "phase_ms": {"projection": proj_kms / 3, "diffusion": diff_kms / 3,
+                     "how": "CUDA events around each phase's own kernels, timed alone; "
+                            "with_copy_back adds the copy to the public fields that a "
+                            "phase called on its own ends with and a step does not run",
+                     "with_copy_back": {"projection": proj_ms / 3, "diffusion": diff_ms / 3}},
         "phase_launches": {"projection": proj_kernels // 3, "diffusion": diff_kernels // 3},
         "wall_s": wall,
         "clocks": clk.summary(),

@@ -273,6 +273,18 @@ int os_profile_phase(os_handle* h, int32_t phase, const os_source* src, float dt
                      int32_t reps, void* stream, float* ms_out, int32_t* kernels_out);
 
 /*
+ * As os_profile_phase, but the time of each repetition is taken only over the
+ * phase's own kernels, as a step runs them: a phase called on its own ends by
+ * copying the velocity back to the public fields when its pass count leaves
+ * it in the other buffers (a step does not), and that copy is left out of
+ * `kernel_ms_out` (summed over the repetitions). `ms_out` is the whole time,
+ * as os_profile_phase gives it. No reference counterpart.
+ */
+int os_profile_phase_kernels(os_handle* h, int32_t phase, const os_source* src, float dt,
+                             int32_t reps, void* stream, float* kernel_ms_out, float* ms_out,
+                             int32_t* kernels_out);
+
+/*
  * The diffusion phase (n Jacobi sweeps of u, as OS_PHASE_DIFFUSION runs it)
  * on a caller-owned device field, without allocating anything. No counterpart
  * in the reference: it is for callers that may not allocate device memory

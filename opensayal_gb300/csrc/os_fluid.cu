@@ -244,6 +244,9 @@ struct Enq {
   cudaStream_t st;
   int count = 0;
   bool failed = false;  // a launch that reports its refusal by return value
+  // Recorded on `st` after a diffusion or projection phase's own kernels,
+  // before the copy back that a phase called on its own may add.
+  cudaEvent_t kernels_done = nullptr;
 };
 
 // Where the live velocity sits while a step is enqueued: 0 = the public
@@ -410,10 +413,12 @@ int enqueue_phase(os_handle* h, int phase, Enq& q) {
       break;
     case OS_PHASE_DIFFUSION:
       enqueue_diffusion<S, A>(h, w, q);
+      if (q.kernels_done) cudaEventRecord(q.kernels_done, st);
       settle(h, w, q);
       break;
     case OS_PHASE_PROJECTION:
       enqueue_projection<S, A>(h, w, q, false);
+      if (q.kernels_done) cudaEventRecord(q.kernels_done, st);
       settle(h, w, q);
       break;
     case OS_PHASE_PRESSURE_RANGE:
@@ -1408,6 +1413,52 @@ int os_run_phase(os_handle* h, int32_t phase, const os_source* src, float dt) {
 int os_kernel_launches(os_handle* h, int64_t* out) {
   if (!h || !out) return set_err(OS_ERR_INVALID, "null argument");
   *out = h->launches;
+  return OS_OK;
+}
+
+int os_profile_phase_kernels(os_handle* h, int32_t phase, const os_source* src, float dt,
+                             int32_t reps, void* stream, float* kernel_ms_out, float* ms_out,
+                             int32_t* kernels_out) {
+  if (!h || !kernel_ms_out || !ms_out || reps < 1) return set_err(OS_ERR_INVALID, "bad argument");
+  int rc = select_device(h);
+  if (rc) return rc;
+  cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : h->stream;
+  if ((rc = push_params(h, src, dt, st))) return rc;
+  std::vector<cudaEvent_t> ev(2 * (size_t)reps + 1, nullptr);
+  for (auto& x : ev)
+    if (cudaEventCreate(&x) != cudaSuccess) {
+      for (auto& y : ev)
+        if (y) cudaEventDestroy(y);
+      return set_err(OS_ERR_CUDA, "profile: event creation failed");
+    }
+  // ev[2r]: repetition r starts; ev[2r+1]: its own kernels done; ev[2reps]: end.
+  Enq q{st};
+  for (int r = 0; r < reps && rc == OS_OK; r++) {
+    cudaEventRecord(ev[2 * r], st);
+    q.kernels_done = ev[2 * r + 1];
+    rc = dispatch_phase(h, phase, q);
+    // Phases without a copy back leave the mark unrecorded: their kernels
+    // are the whole repetition.
+    if (phase != OS_PHASE_DIFFUSION && phase != OS_PHASE_PROJECTION)
+      cudaEventRecord(ev[2 * r + 1], st);
+  }
+  cudaEventRecord(ev[2 * reps], st);
+  cudaError_t e = cudaEventSynchronize(ev[2 * reps]);
+  float kernels_ms = 0.0f, total = 0.0f;
+  for (int r = 0; r < reps && e == cudaSuccess; r++) {
+    float x = 0.0f;
+    e = cudaEventElapsedTime(&x, ev[2 * r], ev[2 * r + 1]);
+    kernels_ms += x;
+  }
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&total, ev[0], ev[2 * reps]);
+  for (auto& x : ev) cudaEventDestroy(x);
+  if (rc) return rc;
+  if (e != cudaSuccess) return set_err(OS_ERR_CUDA, "profile: %s", cudaGetErrorString(e));
+  if ((rc = check_resident(h))) return rc;
+  h->launches += q.count;
+  *kernel_ms_out = kernels_ms;
+  *ms_out = total;
+  if (kernels_out) *kernels_out = q.count;
   return OS_OK;
 }
 

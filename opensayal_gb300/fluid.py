@@ -271,6 +271,19 @@ class Fluid:
                                          C.byref(ms), C.byref(kern)))
         return ms.value, kern.value
 
+    def profile_phase_kernels(self, phase: int, source: Source | None, d_t: float, reps: int,
+                              stream: int | None = None) -> tuple[float, float, int]:
+        """(milliseconds of the phase's own kernels, milliseconds in all, kernels)
+        for `reps` repetitions of one phase: the first leaves out the copy back
+        to the public fields that a diffusion or projection phase called on its
+        own ends with and a step does not run."""
+        src = (source or Source()).to_native()
+        kms, ms, kern = C.c_float(), C.c_float(), C.c_int32()
+        check(self._lib.os_profile_phase_kernels(
+            self._h, int(phase), C.byref(src), C.c_float(d_t), int(reps),
+            C.c_void_p(stream) if stream else None, C.byref(kms), C.byref(ms), C.byref(kern)))
+        return kms.value, ms.value, kern.value
+
     # -- state ---------------------------------------------------------------
     def indx(self, i: int, j: int) -> int:
         return (self.height - j - 1) * self.width + i

@@ -130,6 +130,10 @@ SIGNATURES = [
     ("os_profile_phase", C.c_int, [C.c_void_p, C.c_int32, C.POINTER(OsSource), C.c_float,
                                    C.c_int32, C.c_void_p, C.POINTER(C.c_float),
                                    C.POINTER(C.c_int32)]),
+    ("os_profile_phase_kernels", C.c_int, [C.c_void_p, C.c_int32, C.POINTER(OsSource),
+                                           C.c_float, C.c_int32, C.c_void_p,
+                                           C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                           C.POINTER(C.c_int32)]),
     ("os_diffuse_noalloc", C.c_int, [C.POINTER(OsConfig), C.c_void_p, C.c_float, C.c_void_p]),
     ("os_diagnose", C.c_int, [C.c_void_p, C.c_void_p]),
     ("os_visual_defaults", C.c_int, [C.c_void_p]),

@@ -211,3 +211,10 @@ def test_grids_beyond_int_indices_are_rejected(lib_built):
     h = C.c_void_p()
     assert lib.os_create(C.byref(cfg), C.byref(h)) == native.OS_ERR_INVALID
     assert b"2^31" in lib.os_last_error()
+
+
+def test_kernel_profile_rejects_bad_arguments(lib_built):
+    lib = native.load()
+    k, m = C.c_float(), C.c_float()
+    assert lib.os_profile_phase_kernels(None, 3, None, C.c_float(0.05), 1, None, C.byref(k),
+                                        C.byref(m), None) == native.OS_ERR_INVALID

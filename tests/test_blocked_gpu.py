@@ -130,3 +130,27 @@ def test_diffusion_depth_in_steps_with_resident_projection(gpu):
         b.update(None, cfg.d_t)
     for field in FIELDS:
         assert same_bits(a.download(field), b.download(field)), field
+
+
+@pytest.mark.parametrize("phase", [native.PHASE_PROJECTION, native.PHASE_DIFFUSION])
+def test_phase_kernel_timing_leaves_the_phase_as_run(gpu, phase):
+    """os_profile_phase_kernels times each repetition's own kernels apart from
+    the copy back, and the fields end as after the same phases run one by
+    one."""
+    cfg = scenarios.default_tunnel_config()
+    cfg.projection_block, cfg.projection_resident = 8, 1
+    state = perturbed_state(cfg, 7)
+    a, b = load_lib(cfg, state), load_lib(cfg, state)
+    kms, ms, launches = b.profile_phase_kernels(phase, None, cfg.d_t, 3)
+    for _ in range(3):
+        a.run_phase(phase, None, cfg.d_t)
+    assert 0.0 < kms <= ms
+    _, launches_plain = b.profile_phase(phase, None, cfg.d_t, 3)
+    assert launches == launches_plain
+    for _ in range(3):
+        a.run_phase(phase, None, cfg.d_t)
+    for field in FIELDS:
+        x, y = a.download(field), b.download(field)
+        assert same_bits(x, y), f"{field}: {int((x != y).sum())} cells differ"
+    a.close()
+    b.close()
