@@ -928,6 +928,149 @@ __device__ __forceinline__ void diff_store_owned(const float* A, int tx, int ty,
   }
 }
 
+// ---------------------------------------------------------------------------
+// The same pass with each buffer split by column parity: E[y * kHalfW + k] =
+// u(2k, y) and O[y * kHalfW + k] = u(2k + 1, y), the odd plane right after the
+// even one. A thread owns the column pair (2k, 2k + 1) over a run of rows and
+// carries both columns' rows below and above in registers, so a row of the
+// pair costs the two loads above, the left neighbour of the even column and
+// the right neighbour of the odd one (each the other plane's word at k - 1 or
+// k + 1: lanes take consecutive words) and the two stores: three
+// shared-memory accesses per cell update instead of four.
+// ---------------------------------------------------------------------------
+#ifndef OS_DIFF_INFLIGHT
+#define OS_DIFF_INFLIGHT 8
+#endif
+template <class S>
+__device__ __forceinline__ void diff_stage_in_pairs(float* A, float* B, int tx, int ty,
+                                                    const S* __restrict__ u_in, const Consts& c,
+                                                    int halo, int TX, int TY) {
+  const int RH = TY + 2 * halo;
+  const int gx0 = tx * TX - halo, gy0 = ty * TY - halo;
+  const int W = c.W, H = c.H;
+  const bool vec = ((W & 3) == 0) && ((gx0 & 3) == 0);
+  const int items = RH * kQuads;
+  float* AO = A + RH * kHalfW;
+  float* BO = B + RH * kHalfW;
+  for (int base = threadIdx.x; base < items; base += blockDim.x * OS_DIFF_INFLIGHT) {
+    float4 uq[OS_DIFF_INFLIGHT];
+#pragma unroll
+    for (int r = 0; r < OS_DIFF_INFLIGHT; r++) {
+      const int it = base + r * blockDim.x;
+      const int y = it / kQuads, x = 4 * (it % kQuads);
+      uq[r] = it < items ? load_quad(u_in, W, H, gx0 + x, gy0 + y, vec)
+                         : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+#pragma unroll
+    for (int r = 0; r < OS_DIFF_INFLIGHT; r++) {
+      const int it = base + r * blockDim.x;
+      if (it >= items) break;
+      const int e = (it / kQuads) * kHalfW + 2 * (it % kQuads);
+      const float2 ev = make_float2(uq[r].x, uq[r].z), od = make_float2(uq[r].y, uq[r].w);
+      *reinterpret_cast<float2*>(A + e) = ev;
+      *reinterpret_cast<float2*>(AO + e) = od;
+      *reinterpret_cast<float2*>(B + e) = ev;
+      *reinterpret_cast<float2*>(BO + e) = od;
+    }
+  }
+}
+
+// One run of Jacobi updates of a column pair, rows e0, e0 + kHalfW, ... (n of
+// them, word offsets in a plane), from A into B; do0 / do1 say which of the
+// two columns the sweep updates (each column's left or right neighbour is
+// read only when that column is updated, so no read leaves the region).
+__device__ __forceinline__ void diff_pair_run(const float* __restrict__ AE,
+                                              const float* __restrict__ AO,
+                                              float* __restrict__ BE, float* __restrict__ BO,
+                                              int e0, int n, bool do0, bool do1, float a,
+                                              float den) {
+  float down0 = AE[e0 - kHalfW], down1 = AO[e0 - kHalfW];
+  float c0 = AE[e0], c1 = AO[e0];
+  int e = e0;
+#pragma unroll 4
+  for (int t = 0; t < n; t++, e += kHalfW) {
+    const float up0 = AE[e + kHalfW], up1 = AO[e + kHalfW];
+    const float left = do0 ? AO[e - 1] : 0.0f;   // u(2k - 1)
+    const float right = do1 ? AE[e + 1] : 0.0f;  // u(2k + 2)
+    // src/fluid.cu:178-182: neighbours (i-1, j), (i+1, j), (i, j-1), (i, j+1)
+    if (do0) BE[e] = fma_rn(a, left + c1 + down0 + up0, c0) / den;
+    if (do1) BO[e] = fma_rn(a, c0 + right + down1 + up1, c1) / den;
+    down0 = c0;
+    c0 = up0;
+    down1 = c1;
+    c1 = up1;
+  }
+}
+
+// `sweeps` Jacobi sweeps on the split region, A -> B -> A ...; on return A
+// holds the result. Ends with a barrier.
+__device__ __forceinline__ void diff_sweeps_pairs(float*& A, float*& B, int tx, int ty,
+                                                  const Consts& c,
+                                                  const StepParams* __restrict__ prm, int sweeps,
+                                                  int halo, int TX, int TY) {
+  const int RH = TY + 2 * halo;
+  const int gx0 = tx * TX - halo, gy0 = ty * TY - halo;
+  const int W = c.W, H = c.H;
+  const float d_t = prm->dt;
+  const float a = c.viscosity * d_t / (float)(c.h * c.h);
+  const int k = threadIdx.x % kHalfW;
+  const int groups = blockDim.x / kHalfW;
+  const int x0 = 2 * k, x1 = 2 * k + 1;
+  const int i0 = gx0 + x0, i1 = gx0 + x1;
+  const int y_lo = max(1, 1 - gy0), y_hi = min(RH - 2, H - 2 - gy0);
+  const int chunk = (y_hi - y_lo + groups) / groups;
+  const int r0 = y_lo + (threadIdx.x / kHalfW) * chunk;
+  const int r1 = min(y_hi + 1, r0 + chunk);
+  // Domain interior and not on the region's outer ring.
+  const bool col0 = x0 > 0 && i0 > 0 && i0 < W - 1;
+  const bool col1 = x1 < kRegionW - 1 && i1 > 0 && i1 < W - 1;
+  const float den = fma_rn(4.0f, a, 1.0f);
+  for (int t = 0; t < sweeps; t++) {
+    // Only cells within `reach` (sweeps still to come) of the owned tile can
+    // still influence it.
+    const int reach = sweeps - 1 - t;
+    const int ya = max(r0, halo - reach), yb = min(r1, RH - halo + reach);
+    const bool do0 = col0 && x0 >= halo - reach && x0 < kRegionW - halo + reach;
+    const bool do1 = col1 && x1 >= halo - reach && x1 < kRegionW - halo + reach;
+    if ((do0 || do1) && ya < yb)
+      diff_pair_run(A, A + RH * kHalfW, B, B + RH * kHalfW, ya * kHalfW + k, yb - ya, do0, do1,
+                    a, den);
+    __syncthreads();
+    float* T = A;
+    A = B;
+    B = T;
+  }
+}
+
+// Owned cells of the split region in A back to global.
+template <class S>
+__device__ __forceinline__ void diff_store_owned_pairs(const float* A, int tx, int ty,
+                                                       S* __restrict__ u_out, const Consts& c,
+                                                       int halo, int TX, int TY) {
+  const int gx0 = tx * TX - halo, gy0 = ty * TY - halo;
+  const int W = c.W, H = c.H;
+  const int RH = TY + 2 * halo;
+  const float* AO = A + RH * kHalfW;
+  const bool vec = ((W & 3) == 0) && ((gx0 & 3) == 0);
+  for (int it = threadIdx.x; it < TY * kQuads; it += blockDim.x) {
+    const int y = halo + it / kQuads, x = 4 * (it % kQuads);
+    const int i = gx0 + x, j = gy0 + y;
+    if (j >= H || i >= W) continue;
+    const int e = y * kHalfW + (x >> 1);
+    const float2 ev = *reinterpret_cast<const float2*>(A + e);
+    const float2 od = *reinterpret_cast<const float2*>(AO + e);
+    const float q[4] = {ev.x, od.x, ev.y, od.y};
+    if (vec && x >= halo && x + 3 < halo + TX) {
+      store_quad(u_out, W, H, i, j, true, make_float4(q[0], q[1], q[2], q[3]));
+      continue;
+    }
+    for (int d = 0; d < 4; d++) {
+      if (x + d < halo || x + d >= halo + TX || i + d >= W) continue;
+      st(u_out + cell_index(W, H, i + d, j), q[d]);
+    }
+  }
+}
+
 template <class S>
 __device__ __forceinline__ void diffuse_tile(float* smem, int tx, int ty,
                                              const S* __restrict__ u_in, S* __restrict__ u_out,
@@ -936,10 +1079,10 @@ __device__ __forceinline__ void diffuse_tile(float* smem, int tx, int ty,
   const int RH = TY + 2 * halo;
   float* A = smem;
   float* B = smem + RH * kRegionW + kArrPad;
-  diff_stage_in<S>(A, B, tx, ty, u_in, c, halo, TX, TY);
+  diff_stage_in_pairs<S>(A, B, tx, ty, u_in, c, halo, TX, TY);
   __syncthreads();
-  diff_sweeps(A, B, tx, ty, c, prm, sweeps, halo, TX, TY);
-  diff_store_owned<S>(A, tx, ty, u_out, c, halo, TX, TY);
+  diff_sweeps_pairs(A, B, tx, ty, c, prm, sweeps, halo, TX, TY);
+  diff_store_owned_pairs<S>(A, tx, ty, u_out, c, halo, TX, TY);
 }
 
 template <class S>
