@@ -938,9 +938,10 @@ __device__ __forceinline__ void diff_store_owned(const float* A, int tx, int ty,
 // k + 1: lanes take consecutive words) and the two stores: three
 // shared-memory accesses per cell update instead of four.
 // ---------------------------------------------------------------------------
-#ifndef OS_DIFF_INFLIGHT
-#define OS_DIFF_INFLIGHT 8
-#endif
+// Quads each thread loads before it stores any: with 8, a whole 256 x 74
+// region is in flight at once (one round trip to L2 instead of two).
+constexpr int kDiffInFlight = 8;
+
 template <class S>
 __device__ __forceinline__ void diff_stage_in_pairs(float* A, float* B, int tx, int ty,
                                                     const S* __restrict__ u_in, const Consts& c,
@@ -952,17 +953,17 @@ __device__ __forceinline__ void diff_stage_in_pairs(float* A, float* B, int tx, 
   const int items = RH * kQuads;
   float* AO = A + RH * kHalfW;
   float* BO = B + RH * kHalfW;
-  for (int base = threadIdx.x; base < items; base += blockDim.x * OS_DIFF_INFLIGHT) {
-    float4 uq[OS_DIFF_INFLIGHT];
+  for (int base = threadIdx.x; base < items; base += blockDim.x * kDiffInFlight) {
+    float4 uq[kDiffInFlight];
 #pragma unroll
-    for (int r = 0; r < OS_DIFF_INFLIGHT; r++) {
+    for (int r = 0; r < kDiffInFlight; r++) {
       const int it = base + r * blockDim.x;
       const int y = it / kQuads, x = 4 * (it % kQuads);
       uq[r] = it < items ? load_quad(u_in, W, H, gx0 + x, gy0 + y, vec)
                          : make_float4(0.f, 0.f, 0.f, 0.f);
     }
 #pragma unroll
-    for (int r = 0; r < OS_DIFF_INFLIGHT; r++) {
+    for (int r = 0; r < kDiffInFlight; r++) {
       const int it = base + r * blockDim.x;
       if (it >= items) break;
       const int e = (it / kQuads) * kHalfW + 2 * (it % kQuads);
