@@ -976,15 +976,27 @@ __device__ __forceinline__ void diff_stage_in_pairs(float* A, float* B, int tx, 
   }
 }
 
+// The Jacobi update's division by den = 1 + 4a, as the fast-math division
+// gives it (RCP false), or as the product with the reciprocal __fdividef(1,
+// den) taken once per sweep (RCP true), which gives the same bits for every
+// float input: tests/cpp/reciprocal_product.cu compares the two over all 2^32
+// inputs for the divisors of the tested configurations and a spread of others
+// in [1, 1e6]. The product is used for den below 2^20.
+template <bool RCP>
+__device__ __forceinline__ float jacobi_divide(float x, float den, float rden) {
+  return RCP ? mul_rn(x, rden) : x / den;
+}
+
 // One run of Jacobi updates of a column pair, rows e0, e0 + kHalfW, ... (n of
 // them, word offsets in a plane), from A into B; do0 / do1 say which of the
 // two columns the sweep updates (each column's left or right neighbour is
 // read only when that column is updated, so no read leaves the region).
+template <bool RCP>
 __device__ __forceinline__ void diff_pair_run(const float* __restrict__ AE,
                                               const float* __restrict__ AO,
                                               float* __restrict__ BE, float* __restrict__ BO,
                                               int e0, int n, bool do0, bool do1, float a,
-                                              float den) {
+                                              float den, float rden) {
   float down0 = AE[e0 - kHalfW], down1 = AO[e0 - kHalfW];
   float c0 = AE[e0], c1 = AO[e0];
   int e = e0;
@@ -994,8 +1006,8 @@ __device__ __forceinline__ void diff_pair_run(const float* __restrict__ AE,
     const float left = do0 ? AO[e - 1] : 0.0f;   // u(2k - 1)
     const float right = do1 ? AE[e + 1] : 0.0f;  // u(2k + 2)
     // src/fluid.cu:178-182: neighbours (i-1, j), (i+1, j), (i, j-1), (i, j+1)
-    if (do0) BE[e] = fma_rn(a, left + c1 + down0 + up0, c0) / den;
-    if (do1) BO[e] = fma_rn(a, c0 + right + down1 + up1, c1) / den;
+    if (do0) BE[e] = jacobi_divide<RCP>(fma_rn(a, left + c1 + down0 + up0, c0), den, rden);
+    if (do1) BO[e] = jacobi_divide<RCP>(fma_rn(a, c0 + right + down1 + up1, c1), den, rden);
     down0 = c0;
     c0 = up0;
     down1 = c1;
@@ -1026,6 +1038,8 @@ __device__ __forceinline__ void diff_sweeps_pairs(float*& A, float*& B, int tx, 
   const bool col0 = x0 > 0 && i0 > 0 && i0 < W - 1;
   const bool col1 = x1 < kRegionW - 1 && i1 > 0 && i1 < W - 1;
   const float den = fma_rn(4.0f, a, 1.0f);
+  const float rden = __fdividef(1.0f, den);
+  const bool use_rcp = den < 1048576.0f;
   for (int t = 0; t < sweeps; t++) {
     // Only cells within `reach` (sweeps still to come) of the owned tile can
     // still influence it.
@@ -1033,9 +1047,14 @@ __device__ __forceinline__ void diff_sweeps_pairs(float*& A, float*& B, int tx, 
     const int ya = max(r0, halo - reach), yb = min(r1, RH - halo + reach);
     const bool do0 = col0 && x0 >= halo - reach && x0 < kRegionW - halo + reach;
     const bool do1 = col1 && x1 >= halo - reach && x1 < kRegionW - halo + reach;
-    if ((do0 || do1) && ya < yb)
-      diff_pair_run(A, A + RH * kHalfW, B, B + RH * kHalfW, ya * kHalfW + k, yb - ya, do0, do1,
-                    a, den);
+    if ((do0 || do1) && ya < yb) {
+      if (use_rcp)
+        diff_pair_run<true>(A, A + RH * kHalfW, B, B + RH * kHalfW, ya * kHalfW + k, yb - ya,
+                            do0, do1, a, den, rden);
+      else
+        diff_pair_run<false>(A, A + RH * kHalfW, B, B + RH * kHalfW, ya * kHalfW + k, yb - ya,
+                             do0, do1, a, den, rden);
+    }
     __syncthreads();
     float* T = A;
     A = B;
