@@ -358,7 +358,7 @@ void settle(os_handle* h, Vel<S>& w, Enq& q) {
 // its own instantiation, in which the divisions by the cell size fold away.
 template <class S, class A>
 void launch_velocity_advection(os_handle* h, cudaStream_t st, S* u, S* v, S* ub, S* vb) {
-  const dim3 g2((h->W + 127) / 128, h->H);
+  const dim3 g2((h->W + 127) / 128, (h->H + kAdvRows - 1) / kAdvRows);
   if (h->c.h == 1)
     launch_pdl(h->pdl, k_advect_velocity<S, A, 1>, g2, 128, 0, st, u, v, ub, vb, h->nbr, h->c, h->d_params);
   else
@@ -367,7 +367,7 @@ void launch_velocity_advection(os_handle* h, cudaStream_t st, S* u, S* v, S* ub,
 
 template <class S, class A, bool COPY_U, bool COPY_V>
 void launch_smoke_advection(os_handle* h, cudaStream_t st, S* ub, S* vb, S* s, S* sb, S* u0, S* v0) {
-  const dim3 g2((h->W + 127) / 128, h->H);
+  const dim3 g2((h->W + 127) / 128, (h->H + kAdvRows - 1) / kAdvRows);
   if (h->c.h == 1)
     launch_pdl(h->pdl, k_advect_smoke<S, A, COPY_U, COPY_V, 1>, g2, 128, 0, st, ub, vb, s, sb, u0, v0, h->nbr, h->c, h->d_params);
   else
